@@ -1,0 +1,432 @@
+#!/usr/bin/env python
+"""ROF time-to-gap benchmark of the fused GB300 PDHG path.
+
+Workload (one "step" = one full solve): colour TV denoising, 2048 x 2048 x 3
+fp32, joint Frobenius coupling of the per-pixel 3x2 Jacobian with Huber
+smoothing alpha = 0.01, lambda = 0.05, f from the seeded piecewise-constant
+generator (sigma = 0.1), diagonally preconditioned steps, until the relative
+primal-dual gap is <= 1e-4 (gap checked every --gran iterations).
+
+value   -- milliseconds per solve with f resident in HBM (x, y reset to 0
+           inside the timed region), CUDA events, max over ranks.
+e2e     -- the same solve through the public API PDHG(...).solve(use_gpu=True)
+           from host numpy data: host->device copies of f and the start
+           point, device->host copies of x and y, all inside the timed region.
+roofline-- the dominant fused pass: algorithmic bytes per launch / average
+           launch time (CUDA events on the launching stream) vs the measured
+           HBM copy bandwidth.
+cpu_baseline / --impl reference -- the CPU oracle (a numpy/scipy port of the
+           reference's CPU PDHG, FP64) on the same input.
+
+Multi-GPU: independent replicas (the path does not shard); N ranks each solve
+their own instance, the reported time is the max over ranks.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ROF time-to-gap 1e-4 (ms)"
+UNIT = "ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="opyx", choices=["opyx", "reference"])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--channels", type=int, default=3)
+    ap.add_argument("--huber", type=float, default=0.01)
+    ap.add_argument("--lbd", type=float, default=0.05)
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--gran", type=int, default=5)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    return ap.parse_args()
+
+
+def workload_config(a, world):
+    return {
+        "workload": "colour Huber-TV ROF %dx%dx%d fp32, alpha=%g, lambda=%g, precond steps, "
+                    "until relgap<=%g" % (a.size, a.size, a.channels, a.huber, a.lbd, a.tol),
+        "image": [a.size, a.size, a.channels], "lambda": a.lbd, "huber_alpha": a.huber,
+        "steps": "precond", "tol": a.tol, "gap_check_every": a.gran, "seed": a.seed,
+        "l2": "working set (x, xbar, y, f = %d MB) larger than L2" %
+              (4 * a.size * a.size * a.channels * 5 // 2 ** 20),
+        "parallelism": "replicas x%d" % world,
+    }
+
+
+def make_image(a):
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    return piecewise_constant((a.size, a.size), a.channels, sigma=0.1, seed=a.seed)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler(object):
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace('.', '', 1).isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace('.', '', 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4)
+                          if r[3 + j].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------- GPU arm
+class ResidentSolver(object):
+    """The fused ROF solve with f, x, y, xbar and the workspace resident in HBM."""
+
+    def __init__(self, a, f):
+        from opymize_gb300 import _lib
+        from opymize_gb300.gpuarray import DeviceArray
+        from opymize_gb300.functionals import SSD, HuberL1Norms
+        from opymize_gb300.linear import GradientOp
+        from opymize_gb300.solvers import PDHG
+        self.lib = _lib
+        n, C = a.size, a.channels
+        N = n * n
+        self.N, self.C, self.K = N, C, 2 * C
+        self.gran, self.tol = a.gran, a.tol
+        self.solver = PDHG(SSD(f.reshape(N, C)), HuberL1Norms(N, (C, 2), a.lbd, a.huber),
+                           GradientOp((n, n), C, scheme="forward"))
+        s = self.solver
+        s.constvars.update(theta=1.0, precond=True)
+        self.p = s._rof_problem(np.float32, "precond")
+        self.f = s.g.f_dev(np.float32)
+        self.x = DeviceArray.zeros((N * C,), np.float32)
+        self.y = DeviceArray.zeros((N * 2 * C,), np.float32)
+        self.xbar = DeviceArray.zeros((N * C,), np.float32)
+        wsb = _lib.load().opyx_rof_workspace_size()
+        self.ws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
+        b = _lib.opyx_rof_buffers()
+        b.x, b.xbar, b.y, b.f, b.ws = self.x.ptr, self.xbar.ptr, self.y.ptr, self.f.ptr, self.ws.ptr
+        self.b = b
+        self.info_off = _lib.load().opyx_rof_info_offset() // 8
+        from opymize_gb300.solvers.pdhg import _RofGraph
+        self.graph = _RofGraph(self.p, self.b, self.gran)
+        self.launches = 0
+
+    def solve(self, maxiter=100000):
+        from opymize_gb300.gpuarray import stream_ptr
+        L = self.lib
+        self.x.fill(0.0)
+        self.y.fill(0.0)
+        L.call("opyx_rof_init", self.p, self.b, stream_ptr())
+        self.launches += 3
+        it = 0
+        while it < maxiter:
+            self.graph.launch()
+            self.launches += 2 * self.gran + 1
+            it += self.gran
+            rec = self.ws[self.info_off:self.info_off + 6].get()
+            if abs(rec[5]) < self.tol and max(rec[2], rec[3]) < self.tol:
+                break
+        self.iters, self.relgap = it, float(rec[5])
+        return it
+
+    def time_pass(self, which, reps=20):
+        from opymize_gb300.gpuarray import torch, stream_ptr
+        t = torch()
+        s = t.cuda.current_stream()
+        for _ in range(3):
+            self.lib.call("opyx_rof_pass", self.p, self.b, which, stream_ptr())
+        e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        t.cuda.synchronize()
+        e0.record(s)
+        for _ in range(reps):
+            self.lib.call("opyx_rof_pass", self.p, self.b, which, stream_ptr())
+        e1.record(s)
+        t.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps * 1e-3   # seconds per launch
+
+
+def e2e_solve(a, f):
+    """The public-API call a user makes, host data in and out."""
+    from opymize_gb300.functionals import SSD, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.gpuarray import torch
+    n, C = a.size, a.channels
+    N = n * n
+    s = PDHG(SSD(f.reshape(N, C)), HuberL1Norms(N, (C, 2), a.lbd, a.huber),
+             GradientOp((n, n), C, scheme="forward"))
+    t0 = time.perf_counter()
+    s.solve(steps="precond", precision="float", term_pd_gap=a.tol, granularity=a.gran)
+    x, y = s.state
+    torch().cuda.synchronize()
+    return time.perf_counter() - t0, s, x.nbytes + y.nbytes
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the fused passes from the committed ncu
+    summary (profiles/rof_passes_2048x2048x3.txt), if present."""
+    path = os.path.join(ROOT, "profiles", "rof_passes_2048x2048x3.txt")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch"):
+                _, name, val = line.split()
+                out[name] = float(val)
+    except OSError:
+        pass
+    return out
+
+
+def cpu_sample(a, f, iters_to_gap, sample_iters=4):
+    """Oracle (CPU port of the reference, FP64) on the same input: time
+    `sample_iters` iterations and one gap evaluation, scale to the iteration
+    count of the solve."""
+    import oracle
+    n, C = a.size, a.channels
+    N = n * n
+    so = oracle.PDHG(oracle.SSD(f.reshape(N, C)), oracle.HuberL1Norms(N, (C, 2), a.lbd, a.huber),
+                     oracle.Gradient((n, n), C, "forward"))
+    t0 = time.perf_counter()
+    so.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=sample_iters,
+             granularity=sample_iters)
+    t_total = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    so.pd_gap()
+    t_gap = time.perf_counter() - t1
+    t_iter = (t_total - t_gap) / sample_iters
+    checks = iters_to_gap // a.gran
+    return (t_iter * iters_to_gap + t_gap * checks) * 1e3, t_iter, t_gap
+
+
+def run_gpu_arm(a, world, rank, local):
+    from opymize_gb300.gpuarray import torch
+    t = torch()
+    t.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=t.device("cuda", local))
+    f = make_image(a)
+    rs = ResidentSolver(a, f)
+    for _ in range(max(3, a.warmup)):
+        rs.solve()
+    s = t.cuda.current_stream()
+    launches0 = rs.launches
+    e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        t.cuda.synchronize()
+        e0.record(s)
+        for _ in range(a.steps):
+            rs.solve()
+        e1.record(s)
+        t.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = e0.elapsed_time(e1) / a.steps
+    launches = rs.launches - launches0
+    if dist:
+        v = t.tensor([ms], device="cuda")
+        dist.all_reduce(v, op=dist.ReduceOp.MAX)
+        ms = float(v.item())
+
+    # roofline of the fused passes (precond: no step-size arrays)
+    C, K, N = rs.C, rs.K, rs.N
+    tA, tB = rs.time_pass(0), rs.time_pass(1)
+    bytesA = 4.0 * N * (K + 4 * C)
+    bytesB = 4.0 * N * (C + 2 * K)
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    dom = ("passA", tA, bytesA) if tA >= tB else ("passB", tB, bytesB)
+    ach = dom[2] / dom[1] / 1e9
+    traffic = profile_traffic().get(dom[0])
+    iter_bytes = 4.0 * N * (5 * C + 3 * K)
+    roof = {"bound": "hbm", "kernel": "k_passA (primal)" if dom[0] == "passA" else "k_passB (dual)",
+            "achieved": round(ach, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "traffic": traffic,
+            "algorithmic_bytes_per_launch": dom[2],
+            "passA_us": round(tA * 1e6, 2), "passB_us": round(tB * 1e6, 2),
+            "iteration_GBps": round(iter_bytes / (tA + tB) / 1e9, 1),
+            "iteration_frac": round(iter_bytes / (tA + tB) / 1e9 / peak, 4)}
+
+    # e2e through the public API (rank-local)
+    e2e_times = []
+    for _ in range(2):
+        e2e_solve(a, f)                      # warm
+    for _ in range(max(1, min(a.steps, 3))):
+        dt, s_api, d2h = e2e_solve(a, f)
+        e2e_times.append(dt)
+    h2d = f.size * 4 + s_api.g.x.size * 4 + s_api.f.x.size * 4
+    e2e_ms = float(np.median(e2e_times) * 1e3)
+    if dist:
+        v = t.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(v, op=dist.ReduceOp.MAX)
+        e2e_ms = float(v.item())
+
+    out = None
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded piecewise-constant image + noise)",
+            "config": workload_config(a, world),
+            "iters_to_gap": rs.iters, "final_relgap": rs.relgap,
+            "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "api": "PDHG(SSD, HuberL1Norms, GradientOp).solve(use_gpu=True, "
+                           "steps='precond', precision='float')"},
+            "roofline": roof,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        if world == 1 and not a.no_cpu:
+            cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs.iters)
+            out["cpu_baseline"] = {
+                "value": round(cpu_ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": "oracle PDHG (numpy/scipy port of the reference CPU path, FP64) on "
+                          "the same 2048x2048x3 input: 4 iterations (%.3f s/it) and one gap "
+                          "evaluation (%.3f s) timed, scaled to the %d iterations and %d gap "
+                          "checks of the solve" % (t_iter, t_gap, rs.iters, rs.iters // a.gran),
+                "host_cpus": os.cpu_count()}
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference_arm(a, world, rank):
+    if rank != 0:
+        return None
+    import oracle
+    f = make_image(a)
+    n, C = a.size, a.channels
+    N = n * n
+
+    def problem():
+        return oracle.PDHG(oracle.SSD(f.reshape(N, C)),
+                           oracle.HuberL1Norms(N, (C, 2), a.lbd, a.huber),
+                           oracle.Gradient((n, n), C, "forward"))
+
+    # one full CPU solve to the gap (untimed pass that fixes the iteration
+    # count; its wall time is reported as well)
+    so = problem()
+    t0 = time.perf_counter()
+    so.solve(steps="precond", term_pd_gap=a.tol, term_maxiter=100000, granularity=a.gran)
+    full_s = time.perf_counter() - t0
+    iters = int(so.info["iter"])
+    checks = iters // a.gran
+    sample = 2
+    samples = []
+    for k in range(a.warmup + a.steps):
+        sp = problem()
+        t0 = time.perf_counter()
+        sp.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=sample, granularity=sample)
+        t_it_gap = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        sp.pd_gap()
+        t_gap = time.perf_counter() - t1
+        if k >= a.warmup:
+            samples.append(((t_it_gap - t_gap) / sample, t_gap))
+    t_iter = float(np.median([s[0] for s in samples]))
+    t_gap = float(np.median([s[1] for s in samples]))
+    ms = (t_iter * iters + t_gap * checks) * 1e3
+    return {
+        "metric": METRIC, "value": round(ms, 1), "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms, 1),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded piecewise-constant image + noise)",
+        "config": workload_config(a, world), "impl": "reference",
+        "iters_to_gap": iters, "full_solve_ms": round(full_s * 1e3, 1),
+        "cpu_baseline": {"value": round(ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "each step: %d iterations + 1 gap evaluation of the oracle "
+                                   "(numpy/scipy port of the reference CPU PDHG) on the full "
+                                   "input, scaled to the %d iterations / %d checks its own "
+                                   "untimed full solve needed (%.1f s)" % (sample, iters, checks,
+                                                                            full_s),
+                         "host_cpus": os.cpu_count()},
+        "e2e": {"value": round(ms, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_setup()
+    if a.impl == "reference":
+        out = run_reference_arm(a, world, rank)
+    else:
+        out = run_gpu_arm(a, world, rank, local)
+    if out is not None:
+        print(json.dumps(out))
+        sys.stdout.flush()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,335 @@
+/*
+ * opyx.h -- C ABI of libopyx, the GB300 (sm_103a) kernels behind
+ * opymize_gb300's PDHG path.
+ *
+ * Every entry point replaces one kernel (or kernel family) that the reference
+ * compiles at run time through PyCUDA (opymize/tools/gpu.py:39-80,
+ * `prepare_kernels` -> `{name: kernelfun(*gpudata)}`), and is what a binding
+ * of that path would call instead.  Conventions:
+ *
+ *   - all array arguments are DEVICE pointers owned by the caller; the library
+ *     never allocates memory (scratch comes from caller-sized workspaces);
+ *   - `dtype` is OPYX_F32 or OPYX_F64 and applies to every iterate array of
+ *     the call; constant operator data (weights, matrices) is double;
+ *   - `add` = 0 writes the result, `add` = 1 accumulates into the target,
+ *     as `Operator.__call__(x, y, add=...)` (opymize/__init__.py:64-84);
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream); calls are
+ *     asynchronous and capturable in a CUDA graph unless stated otherwise;
+ *   - every function returns an int status (OPYX_OK = 0); nothing throws
+ *     across the ABI.
+ */
+#ifndef OPYX_H
+#define OPYX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  OPYX_OK = 0,
+  OPYX_ERR_ARG = 1,           /* bad shape, size, pointer or enum value      */
+  OPYX_ERR_LAUNCH = 2,        /* CUDA launch / runtime error                  */
+  OPYX_ERR_UNSUPPORTED = 3,   /* valid request this build does not implement */
+  OPYX_ERR_WORKSPACE = 4,     /* workspace too small or misaligned           */
+  OPYX_ERR_NOT_CONVERGED = 5  /* an iterative device routine hit its bound   */
+};
+
+enum { OPYX_F32 = 0, OPYX_F64 = 1 };
+
+/* Library version (major*10000 + minor*100 + patch). */
+int opyx_version(void);
+/* Static description of a status code. */
+const char* opyx_status_string(int status);
+/* Number of SMs of the current device (grid sizing). */
+int opyx_sm_count(void);
+
+/* ------------------------------------------------------------ utilities */
+/* y[i] = value  (gpuarray.fill, used before every reference LinOp call:
+ * opymize/linear/diff.py:143, :182). */
+int opyx_fill(int dtype, void* y, int64_t n, double value, void* stream);
+/* y = a*x + b*y  (gpuarray `y[:] = x`, `y += x`, ScaleOp; scale.py:44-67). */
+int opyx_axpby(int dtype, int64_t n, double a, const void* x, double b, void* y,
+               void* stream);
+/* y = |x| elementwise (numpy `np.abs`, power iteration of normest:
+ * opymize/linear/__init__.py:11-46). */
+int opyx_abs(int dtype, int64_t n, const void* x, void* y, void* stream);
+/* x_i <- 1/x_i where x_i > eps, unchanged elsewhere: the diagonal
+ * preconditioners from rowwise norms (opymize/solvers/pdhg.py:197-198). */
+int opyx_recip_positive(int dtype, int64_t n, void* x, double eps, void* stream);
+/* y[(o*N + i)*inner + r] (+)= pat[o*inner + r]: broadcasts a small per-row
+ * pattern (rowwise norms of per-pixel operators) over N pixels. */
+int opyx_broadcast_mid(int dtype, const double* pat, int64_t outer, int64_t N,
+                       int64_t inner, void* y, int add, void* stream);
+/* out[0] = sum_i x_i^2, out[1] = max_i |x_i| in FP64 (device double[2]);
+ * `ws` >= opyx_reduce_workspace_size() bytes. */
+size_t opyx_reduce_workspace_size(void);
+int opyx_norms(int dtype, int64_t n, const void* x, double* out, void* ws,
+               void* stream);
+
+/* ---------------------------------------------- finite differences (diff) */
+#define OPYX_MAX_DIMS 6
+typedef struct {
+  int32_t ndim;                 /* D, 1..OPYX_MAX_DIMS                      */
+  int32_t nchannels;            /* C >= 1                                   */
+  int64_t dims[OPYX_MAX_DIMS];  /* image shape, row-major, last contiguous  */
+  double h[OPYX_MAX_DIMS];      /* grid step per axis (imageh)              */
+} opyx_grid;
+
+enum { OPYX_SCHEME_FORWARD = 0, OPYX_SCHEME_CENTERED = 1 };
+
+/* y[i,t,k] (+)= D x : GradientOp (opymize/linear/diff.py:67-144), kernel
+ * `gradient` (opymize/linear/diff.cu:37-75).  x is (N, C), y is (N, D, C);
+ * `weights` is a device double[C] or NULL (all ones). */
+int opyx_gradient(const opyx_grid* g, int scheme, const double* weights, int dtype,
+                  const void* x, void* y, int add, void* stream);
+/* x (+)= D^T y : DivergenceOp (diff.py:146-183), kernel `divergence`
+ * (diff.cu:77-127). */
+int opyx_divergence(const opyx_grid* g, int scheme, const double* weights, int dtype,
+                    const void* y, void* x, int add, void* stream);
+/* Rowwise l^p norms of the gradient (transpose = 0, y of size N*D*C) or of
+ * the divergence (transpose = 1, y of size N*C):  y_i (+)= (sum_j |A_ij|^p)^(1/p),
+ * as LinOp.rowwise_lp on the reference's sparse matrix (opymize/__init__.py:122-142). */
+int opyx_gradient_rowlp(const opyx_grid* g, int scheme, const double* weights,
+                        int transpose, double p, int dtype, void* y, int add,
+                        void* stream);
+
+enum { OPYX_BC_NEUMANN = 0, OPYX_BC_CURVATURE = 1, OPYX_BC_SECOND_ORDER = 2 };
+/* y (+)= Laplacian x with boundary `bc` (or its adjoint):  LaplacianOp
+ * (diff.py:185-249), kernel `laplacian` (diff.cu:131-243). */
+int opyx_laplacian(const opyx_grid* g, int bc, int adjoint, int dtype,
+                   const void* x, void* y, int add, void* stream);
+int opyx_laplacian_rowlp(const opyx_grid* g, int bc, int adjoint, double p,
+                         int dtype, void* y, int add, void* stream);
+
+/* -------------------------------------------- per-pixel products (einsum) */
+/* y_ji (+)= sum_k A_jk x_ki, x (K,N), y (J,N); trans: A stored (K,J).
+ * MatrixMult (opymize/linear/einsum.py:17-56), kernel `matrixmult`
+ * (einsum.cu:3-28).  A is a device double array. */
+int opyx_matrixmult(int dtype, int64_t N, int J, int K, const double* A, int trans,
+                    const void* x, void* y, int add, void* stream);
+/* y_ij (+)= sum_k x_ik A_kj, x (N,K), y (N,J); trans: A stored (J,K).
+ * MatrixMultR (einsum.py:58-97), kernel `matrixmultr` (einsum.cu:32-57). */
+int opyx_matrixmultr(int dtype, int64_t N, int K, int J, const double* A, int trans,
+                     const void* x, void* y, int add, void* stream);
+/* y_jlk (+)= sum_m x_jlm A_jmk, x (J,L,M), y (J,L,K); trans: A stored (J,K,M).
+ * MatrixMultRBatched (einsum.py:175-214), kernel `matrixmultrbatched`
+ * (einsum.cu:61-87). */
+int opyx_matrixmultr_batched(int dtype, int J, int64_t L, int M, int K,
+                             const double* A, int trans, const void* x, void* y,
+                             int add, void* stream);
+/* y_mik (+)= sum_jl x_jil A_jlmk, x (J,N,L), y (M,N,K); trans: A stored
+ * (M,K,J,L).  TangledMatrixMultR (einsum.py:130-173), kernel
+ * `tangledmatrixmultr` (einsum.cu:91-122). */
+int opyx_tangled_matrixmultr(int dtype, int J, int64_t N, int L, int M, int K,
+                             const double* A, int trans, const void* x, void* y,
+                             int add, void* stream);
+/* y_ik (+)= x_ik A_k.  DiagMatrixMultR (einsum.py:104-128). */
+int opyx_diag_matrixmultr(int dtype, int64_t N, int K, const double* A,
+                          const void* x, void* y, int add, void* stream);
+
+/* ------------------------------------------------- label gather / scatter */
+/* y[j,i,m] (+)= -sum_l B[j,m,l] x[i,P[j,l]], x (N,K), y (J,N,M); B device
+ * double (J,M,L), P device int64 (J,L).  IndexedMult
+ * (opymize/linear/indexed.py:63-94), kernel `indexedmult` (indexed.cu:28-48). */
+int opyx_indexedmult(int dtype, int J, int64_t N, int M, int L, int K,
+                     const double* B, const int64_t* P, const void* x, void* y,
+                     int add, void* stream);
+/* y[i,P[j,l]] (+)= -sum_m B[j,m,l] x[j,i,m]: IndexedMultAdj
+ * (indexed.py:34-61), kernel `indexedmultadj` (indexed.cu:2-26). */
+int opyx_indexedmult_adj(int dtype, int J, int64_t N, int M, int L, int K,
+                         const double* B, const int64_t* P, const void* x, void* y,
+                         int add, void* stream);
+
+/* ------------------------------------------------------------- step sizes */
+/* A step size is a per-element device vector (`vec`, of the iterate dtype,
+ * preconditioned steps), else a device double written by the solver
+ * (`dev`, adaptive steps), else the constant `value`. */
+typedef struct {
+  const void* vec;
+  const double* dev;
+  double value;
+} opyx_step;
+
+/* ----------------------------------------------------------- prox maps */
+/* y (+)= a*(x + b*shift) with each of a, b, shift a device vector of the
+ * iterate dtype or (NULL) the scalar given.  ShiftScaleOp
+ * (opymize/operators/affine.py:85-146). */
+int opyx_shiftscale(int dtype, int64_t n, const void* a_vec, double a,
+                    const void* b_vec, double b, const void* shift_vec, double shift,
+                    const void* x, void* y, int add, void* stream);
+/* SSD prox: y = (x + t*f)/(1 + t) with t = tau*vol_k on masked pixels, y = x
+ * elsewhere; x, y, f (N,C); vol device double[C] (NULL = ones); mask device
+ * uint8[N] (NULL = all).  SSD.prox -> ShiftScaleOp (functionals/quad.py:45-55). */
+int opyx_ssd_prox(int dtype, int64_t N, int C, const void* f, const double* vol,
+                  const uint8_t* mask, opyx_step tau, const void* x, void* y,
+                  void* stream);
+/* y (+)= max(0,x) / min(0,x): PosProj / NegProj (operators/proj.py:19-85). */
+int opyx_posproj(int dtype, int64_t n, const void* x, void* y, int add, void* stream);
+int opyx_negproj(int dtype, int64_t n, const void* x, void* y, int add, void* stream);
+/* y (+)= mask[i] ? c[i,:] : x[i,:] for (N,M) data: ConstrainOp
+ * (operators/affine.py:46-83). */
+int opyx_constrain(int dtype, int64_t N, int M, const uint8_t* mask, const void* c,
+                   const void* x, void* y, int add, void* stream);
+
+enum { OPYX_NORM_FROBENIUS = 0, OPYX_NORM_SPECTRAL = 1 };
+/* In-place projection of each x_i (an M1 x M2 matrix) onto the ball of
+ * radius lbd in the Frobenius norm or (2 x M / M x 2 only) the spectral norm.
+ * L1NormsProj (operators/proj.py:170-226), kernel `l1normsproj`
+ * (operators/proj.cu:2-108). */
+int opyx_l1normsproj(int dtype, int64_t N, int M1, int M2, double lbd, int matrixnorm,
+                     void* x, void* stream);
+/* In-place prox of sigma*F* for F = lbd*sum_i huber_alpha(|x_i|_F):
+ * x_i <- proj_{|.|_F<=lbd}(x_i / (1 + sigma*alpha/lbd)), groups of m values. */
+int opyx_huber_conj_prox(int dtype, int64_t N, int m, double lbd, double alpha,
+                         opyx_step sigma, void* x, void* stream);
+/* In-place projection of (x1, x2) in R^M x R onto the epigraph of
+ * 0.5*alph*|x1 - s1|^2 + s2 (shift s device (N, M+1) of the iterate dtype or
+ * NULL), truncated at |x1 - s1| <= lbd when lbd is finite.  The cubic
+ * root-finding runs in FP64 for both dtypes.  QuadEpiProj
+ * (operators/proj.py:278-374), kernel `quadepiproj` (operators/proj.cu:110-220). */
+int opyx_quadepiproj(int dtype, int64_t N, int M, double alph, const void* shift,
+                     double lbd, void* x, void* stream);
+
+/* --------------------------------------------------- generic PDHG steps */
+/* zkp1 = zk + direction*step*zgrad: `take_step` (opymize/solvers/pdhg.py:62-65). */
+int opyx_take_step(int dtype, int64_t n, void* zkp1, const void* zk, int direction,
+                   opyx_step step, const void* zgrad, void* stream);
+/* ykp1 = yk + sigma*((1+theta)*ygkp1 - theta*ygk): `overrelax` followed by
+ * `take_step` (pdhg.py:66-69, :145-151) in one pass. */
+int opyx_dual_step(int dtype, int64_t n, void* ykp1, const void* yk, opyx_step sigma,
+                   double theta, const void* ygkp1, const void* ygk, void* stream);
+/* out[0] += sum((zk - zkp1)/a - b*zgk + c1*zgkp1)^2,
+ * out[1] += sum((zk - zkp1)/a - b*zgk + c2*zgkp1)^2 in FP64: two `residual`
+ * reductions (pdhg.py:74-78) sharing their reads.  `out` is device double[2]
+ * (accumulated), `ws` a reduction workspace. */
+int opyx_residual_pair(int dtype, int64_t n, opyx_step a, const void* zk,
+                       const void* zkp1, double b, const void* zgk, double c1,
+                       double c2, const void* zgkp1, double* out, void* ws,
+                       void* stream);
+
+/* Device state of the adaptive step rule (pdhg.py:156-183), all double. */
+typedef struct {
+  double tau, sigma, alpha;       /* current steps and damping              */
+  double eta, Delta, theta;       /* constants (0.95, 1.5, 1.0)             */
+  double eps[4];                  /* eps_abs_p, eps_rel_p, eps_abs_d, eps_rel_d */
+  double sums[4];                 /* |r_p|^2, |g_p|^2, |r_d|^2, |g_d|^2 (accumulated) */
+  double resp, resd, epsp, epsd;  /* outputs of the last update             */
+  double xsize, ysize;            /* primal and dual sizes                  */
+} opyx_adaptive_state;
+
+/* Apply the adaptive rule to `st` (device pointer) from its `sums`, then
+ * zero the sums.  Single-thread kernel; no host synchronisation. */
+int opyx_adaptive_update(opyx_adaptive_state* st, void* stream);
+
+/* ------------------------------------------------ functional evaluation */
+/* Value and infeasibility of a functional at x, reduced in FP64 on the
+ * device (the reference evaluates them in numpy on the host for the gap,
+ * opymize/solvers/pdhg.py:23-44, :292-301).  x holds `ngroups` groups of
+ * m1*m2 values; out is a device double[2] = {val, infeas}; ws is a reduction
+ * workspace (opyx_reduce_workspace_size bytes, zero-filled before first use). */
+enum {
+  OPYX_FCT_SSD = 0,          /* functionals/quad.py:7-43; v0 = f, vol, mask, scalar0 = shift */
+  OPYX_FCT_L1NORMS,          /* l1norms.py:34-63; lbd, matrixnorm SPECTRAL = nuclear   */
+  OPYX_FCT_L1NORMS_CONJ,     /* l1norms.py:65-88; lbd, matrixnorm                     */
+  OPYX_FCT_HUBER,            /* lbd*sum huber_alpha(|x_i|)                            */
+  OPYX_FCT_HUBER_CONJ,       /* alpha/(2 lbd) sum |x_i|^2 + indicator(|x_i| <= lbd)     */
+  OPYX_FCT_QUADEPI_IND,      /* epigraph.py:169-197; a, v0 = b (N,M), v1 = c (N)        */
+  OPYX_FCT_QUADEPI_SUPP,     /* epigraph.py:135-166; a, v0 = b, v1 = c                 */
+  OPYX_FCT_HUBER_PERSP,      /* epigraph.py:203-236; lbd, alpha                         */
+  OPYX_FCT_TRUNCQUAD_IND,    /* epigraph.py:238-270; lbd, alpha                         */
+  OPYX_FCT_POSITIVITY,       /* indicators.py:74-93                                    */
+  OPYX_FCT_NEGATIVITY,       /* indicators.py:95-98                                    */
+  OPYX_FCT_AFFINE,           /* functionals/affine.py:9-44; scalar0 = b, v0 or scalar1 = c */
+  OPYX_FCT_INDICATOR,        /* indicators.py:8-29; v0 or scalar1 = c1, scalar0 = c2   */
+  OPYX_FCT_CONSTRAIN,        /* indicators.py:31-58; mask, v0 = c                       */
+  OPYX_FCT_MASKED_AFFINE     /* functionals/affine.py:59-90; mask, v0 = c               */
+};
+
+typedef struct {
+  int32_t kind;
+  int32_t matrixnorm;
+  int64_t ngroups;
+  int32_t m1, m2;
+  double lbd, alpha, a;
+  double scalar0, scalar1;
+  const void* v0;            /* iterate dtype, or NULL */
+  const void* v1;            /* iterate dtype, or NULL */
+  const double* vol;         /* device double[m1*m2] or NULL */
+  const uint8_t* mask;       /* device uint8[ngroups] or NULL */
+} opyx_fct;
+
+int opyx_fct_eval(const opyx_fct* f, int dtype, const void* x, double* out, void* ws,
+                  void* stream);
+
+/* ------------------------------------------------ fused ROF-type PDHG path */
+/* min_x G(x) + F(Ax) with G = SSD(f, vol, mask, shift), F = lbd*L1Norms
+ * (Frobenius) or its Huber smoothing, A = forward-difference GradientOp:
+ * PDHG.solve(use_gpu=True) for this (G, F, A) (opymize/solvers/pdhg.py:229-315,
+ * functionals/quad.py, functionals/l1norms.py, linear/diff.py) with each
+ * iteration fused into two passes (three for adaptive steps). */
+#define OPYX_ROF_MAX_C 4
+enum { OPYX_STEPS_CONST = 0, OPYX_STEPS_ADAPTIVE = 1, OPYX_STEPS_PRECOND = 2 };
+
+typedef struct {
+  int32_t dtype;                    /* OPYX_F32 / OPYX_F64                   */
+  int32_t ndim;                     /* D, 1..3                               */
+  int32_t nchannels;                /* C, 1..OPYX_ROF_MAX_C                  */
+  int32_t steps;                    /* OPYX_STEPS_*                          */
+  int64_t dims[3];                  /* image shape (dims[0..D-1])            */
+  double h[3];                      /* grid steps (GradientOp imageh)        */
+  double weights[OPYX_ROF_MAX_C];   /* GradientOp channel weights            */
+  double vol[OPYX_ROF_MAX_C];       /* SSD volume element per channel        */
+  double ssd_shift;                 /* SSD constant                          */
+  double lbd;                       /* regularisation weight (> 0)           */
+  double huber_alpha;               /* 0: L1Norms; > 0: Huber parameter      */
+  double tau, sigma;                /* initial steps (constant / adaptive)   */
+  double theta;                     /* overrelaxation (the reference uses 1) */
+  double alpha0, eta, Delta;        /* adaptive rule (0.5, 0.95, 1.5)        */
+  double eps[4];                    /* adaptive tolerances (pdhg.py:275-280) */
+} opyx_rof_problem;
+
+typedef struct {
+  void* x;              /* (N, C) primal iterate, updated in place           */
+  void* xbar;           /* (N, C) extrapolated primal                        */
+  void* y;              /* (N, D, C) dual iterate, updated in place          */
+  const void* f;        /* (N, C) data                                       */
+  const uint8_t* mask;  /* (N) SSD mask or NULL                              */
+  void* xgrad;          /* (N, C) adaptive steps only: A^T y (else NULL)     */
+  void* gp;             /* (N, C) adaptive steps only: residual part         */
+  void* ws;             /* workspace of opyx_rof_workspace_size() bytes,
+                           256-byte aligned, zero-filled once before its
+                           first use                                         */
+} opyx_rof_buffers;
+
+/* Values of the last opyx_rof_gap (pdhg.py:23-44) and of the step state. */
+typedef struct {
+  double objp, objd, infeasp, infeasd, gap, relgap;
+  double tau, sigma, alpha, resp, resd, epsp, epsd;
+} opyx_rof_info;
+
+size_t opyx_rof_workspace_size(void);
+/* Byte offset of the opyx_rof_info record inside the workspace. */
+size_t opyx_rof_info_offset(void);
+/* Validate and set up: device step state from `p`; for adaptive steps also
+ * xgrad = A^T y of the initial y.  x, y hold the starting point. */
+int opyx_rof_init(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);
+/* Run `iters` PDHG iterations (pdhg.py:124-187). */
+int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                     void* stream);
+/* One pass of an iteration (0 = primal pass A, 1 = dual pass B, 2 = the
+ * adaptive residual pass R), for per-kernel timing and profiling. */
+int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
+                  void* stream);
+/* Primal-dual gap of the current iterate into the workspace's info record
+ * (FP64 device reductions; pdhg.py:23-44, :287-305). */
+int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPYX_H */

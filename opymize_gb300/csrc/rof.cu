@@ -1,0 +1,255 @@
+// Host side of the fused ROF path: validation, workspace layout, dispatch
+// over (dtype, D, C) and the per-iteration launch sequence.
+#include <string.h>
+
+#include "rof_kernels.cuh"
+
+namespace opyx {
+namespace rof {
+
+// Workspace layout (bytes): [0, 256) adaptive state, [256, 512) info record,
+// [512, 512 + kPartials) FP64 block partials, then the ticket word.
+constexpr size_t kStateOff = 0;
+constexpr size_t kInfoOff = 256;
+constexpr int kMaxBlocks = 4096;
+constexpr size_t kPartialsOff = 512;
+constexpr size_t kPartialsBytes = (size_t)kMaxBlocks * 5 * sizeof(double);
+constexpr size_t kTicketOff = kPartialsOff + kPartialsBytes;
+constexpr size_t kWsBytes = kTicketOff + 256;
+
+static_assert(sizeof(opyx_adaptive_state) <= 256, "state record too large");
+static_assert(sizeof(opyx_rof_info) <= 256, "info record too large");
+
+static int validate(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  if (!p || !b) return OPYX_ERR_ARG;
+  if (p->dtype != OPYX_F32 && p->dtype != OPYX_F64) return OPYX_ERR_ARG;
+  if (p->ndim < 1 || p->ndim > 3) return OPYX_ERR_UNSUPPORTED;
+  if (p->nchannels < 1 || p->nchannels > OPYX_ROF_MAX_C) return OPYX_ERR_UNSUPPORTED;
+  if (p->steps < OPYX_STEPS_CONST || p->steps > OPYX_STEPS_PRECOND) return OPYX_ERR_ARG;
+  for (int t = 0; t < p->ndim; ++t)
+    if (p->dims[t] < 1 || !(p->h[t] > 0)) return OPYX_ERR_ARG;
+  for (int k = 0; k < p->nchannels; ++k)
+    if (!(p->vol[k] > 0)) return OPYX_ERR_ARG;
+  if (!(p->lbd > 0) || p->huber_alpha < 0 || !(p->theta > 0)) return OPYX_ERR_ARG;
+  if (p->steps != OPYX_STEPS_PRECOND && (!(p->tau > 0) || !(p->sigma > 0))) return OPYX_ERR_ARG;
+  if (p->steps == OPYX_STEPS_ADAPTIVE &&
+      (!(p->alpha0 > 0) || !(p->alpha0 < 1) || !(p->Delta > 1) || !(p->eta > 0)))
+    return OPYX_ERR_ARG;
+  if (!b->x || !b->xbar || !b->y || !b->f || !b->ws) return OPYX_ERR_ARG;
+  if (p->steps == OPYX_STEPS_ADAPTIVE && (!b->xgrad || !b->gp)) return OPYX_ERR_ARG;
+  if (((uintptr_t)b->ws) & 255) return OPYX_ERR_WORKSPACE;
+  const size_t al = p->dtype == OPYX_F32 ? 4 : 8;
+  if (((uintptr_t)b->x | (uintptr_t)b->xbar | (uintptr_t)b->y | (uintptr_t)b->f) & (al - 1))
+    return OPYX_ERR_ARG;
+  return OPYX_OK;
+}
+
+static Geo make_geo(const opyx_rof_problem* p) {
+  Geo g;
+  const int D = p->ndim;
+  g.N = 1;
+  for (int t = 0; t < 3; ++t) { g.n[t] = 1; g.s[t] = 1; g.invh[t] = 1.0; }
+  for (int t = 0; t < D; ++t) { g.n[t] = p->dims[t]; g.invh[t] = 1.0 / p->h[t]; g.N *= p->dims[t]; }
+  int64_t s = 1;
+  for (int t = D - 1; t >= 0; --t) { g.s[t] = s; s *= g.n[t]; }
+  g.nl = g.n[D - 1];
+  g.rows = g.N / g.nl;
+  for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
+    g.w[k] = k < p->nchannels ? p->weights[k] : 1.0;
+    g.vol[k] = k < p->nchannels ? p->vol[k] : 1.0;
+  }
+  g.lbd = p->lbd;
+  g.huber = p->huber_alpha;
+  g.theta = p->theta;
+  g.steps = p->steps;
+  return g;
+}
+
+template <typename T>
+static Args<T> make_args(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  Args<T> a;
+  a.x = (T*)b->x;
+  a.xbar = (T*)b->xbar;
+  a.y = (T*)b->y;
+  a.f = (const T*)b->f;
+  a.mask = b->mask;
+  a.xgrad = (T*)b->xgrad;
+  a.gp = (T*)b->gp;
+  char* ws = (char*)b->ws;
+  a.st = (opyx_adaptive_state*)(ws + kStateOff);
+  a.info = (opyx_rof_info*)(ws + kInfoOff);
+  a.partials = (double*)(ws + kPartialsOff);
+  a.ticket = (unsigned*)(ws + kTicketOff);
+  a.tau = p->tau;
+  a.sigma = p->sigma;
+  return a;
+}
+
+// Launch shape: 32 x 8 threads; x covers the contiguous axis, y-blocks run
+// grid-stride over the remaining rows.  Reduction kernels cap the number of
+// blocks at kMaxBlocks (their partials buffer).
+static void shape(const Geo& g, dim3* grid, dim3* block, bool reduce) {
+  *block = dim3(32, 8, 1);
+  const int64_t cap_total = reduce ? kMaxBlocks : (int64_t)sm_count() * 64;
+  int64_t gx = (g.nl + 31) / 32;
+  if (gx > cap_total) gx = cap_total;          // the kernels grid-stride along x too
+  int64_t gy = (g.rows + 7) / 8;
+  int64_t cap_y = cap_total / gx;
+  if (cap_y < 1) cap_y = 1;
+  if (gy > cap_y) gy = cap_y;
+  if (gy > 65535) gy = 65535;
+  *grid = dim3((unsigned)gx, (unsigned)gy, 1);   // gx * gy <= cap_total
+}
+
+template <typename T, int D, int C>
+struct Runner {
+  static int init(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
+    Geo g = make_geo(p);
+    Args<T> a = make_args<T>(p, b);
+    if (p->steps == OPYX_STEPS_ADAPTIVE) {
+      dim3 grid, block;
+      shape(g, &grid, &block, false);
+      k_passR<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+      return check_launch();
+    }
+    return OPYX_OK;
+  }
+
+  static int iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                     cudaStream_t s) {
+    Geo g = make_geo(p);
+    Args<T> a = make_args<T>(p, b);
+    dim3 grid, block, rgrid, rblock;
+    shape(g, &grid, &block, false);
+    shape(g, &rgrid, &rblock, true);
+    for (int it = 0; it < iters; ++it) {
+      if (p->steps == OPYX_STEPS_ADAPTIVE) {
+        k_passA<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+        k_passB<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+        k_passR<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+      } else {
+        k_passA<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+        k_passB<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+      }
+    }
+    return check_launch();
+  }
+
+  static int pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
+                  cudaStream_t s) {
+    Geo g = make_geo(p);
+    Args<T> a = make_args<T>(p, b);
+    dim3 grid, block, rgrid, rblock;
+    shape(g, &grid, &block, false);
+    shape(g, &rgrid, &rblock, true);
+    const bool ad = p->steps == OPYX_STEPS_ADAPTIVE;
+    if (which == 0) {
+      if (ad) k_passA<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+      else k_passA<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+    } else if (which == 1) {
+      if (ad) k_passB<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+      else k_passB<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+    } else if (which == 2 && ad) {
+      k_passR<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
+    } else {
+      return OPYX_ERR_ARG;
+    }
+    return check_launch();
+  }
+
+  static int gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
+    Geo g = make_geo(p);
+    Args<T> a = make_args<T>(p, b);
+    dim3 grid, block;
+    shape(g, &grid, &block, true);
+    k_gap<T, D, C><<<grid, block, 0, s>>>(g, a, p->ssd_shift);
+    return check_launch();
+  }
+};
+
+template <typename F>
+static int dispatch(const opyx_rof_problem* p, F&& f) {
+#define OPYX_ROF_CASE(TT, DD, CC)                                            \
+  if (p->ndim == DD && p->nchannels == CC) return f(Runner<TT, DD, CC>());
+#define OPYX_ROF_CASES(TT)                                                   \
+  OPYX_ROF_CASE(TT, 1, 1) OPYX_ROF_CASE(TT, 1, 2) OPYX_ROF_CASE(TT, 1, 3) OPYX_ROF_CASE(TT, 1, 4) \
+  OPYX_ROF_CASE(TT, 2, 1) OPYX_ROF_CASE(TT, 2, 2) OPYX_ROF_CASE(TT, 2, 3) OPYX_ROF_CASE(TT, 2, 4) \
+  OPYX_ROF_CASE(TT, 3, 1) OPYX_ROF_CASE(TT, 3, 2) OPYX_ROF_CASE(TT, 3, 3) OPYX_ROF_CASE(TT, 3, 4)
+  if (p->dtype == OPYX_F32) { OPYX_ROF_CASES(float) }
+  else { OPYX_ROF_CASES(double) }
+#undef OPYX_ROF_CASES
+#undef OPYX_ROF_CASE
+  return OPYX_ERR_UNSUPPORTED;
+}
+
+__global__ void k_write_state(opyx_adaptive_state* dst, opyx_adaptive_state v) { *dst = v; }
+
+// Device state record written at init.
+static void host_state(const opyx_rof_problem* p, opyx_adaptive_state* st) {
+  memset(st, 0, sizeof(*st));
+  st->tau = p->tau;
+  st->sigma = p->sigma;
+  st->alpha = p->alpha0;
+  st->eta = p->eta;
+  st->Delta = p->Delta;
+  st->theta = p->theta;
+  for (int j = 0; j < 4; ++j) st->eps[j] = p->eps[j];
+  int64_t N = 1;
+  for (int t = 0; t < p->ndim; ++t) N *= p->dims[t];
+  st->xsize = (double)(N * p->nchannels);
+  st->ysize = (double)(N * p->nchannels * p->ndim);
+}
+
+}  // namespace rof
+}  // namespace opyx
+
+using namespace opyx;
+using namespace opyx::rof;
+
+extern "C" {
+
+size_t opyx_rof_workspace_size(void) { return kWsBytes; }
+size_t opyx_rof_info_offset(void) { return kInfoOff; }
+
+int opyx_rof_init(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream) {
+  int st = validate(p, b);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  // The state record is passed by value through a kernel argument so that
+  // init stays capturable and needs no pinned staging buffer.
+  opyx_adaptive_state hs;
+  host_state(p, &hs);
+  if (cudaMemsetAsync((char*)b->ws + kInfoOff, 0, 256, s) != cudaSuccess) return OPYX_ERR_LAUNCH;
+  if (cudaMemsetAsync((char*)b->ws + kTicketOff, 0, 256, s) != cudaSuccess) return OPYX_ERR_LAUNCH;
+  k_write_state<<<1, 1, 0, s>>>((opyx_adaptive_state*)((char*)b->ws + kStateOff), hs);
+  st = check_launch();
+  if (st) return st;
+  return dispatch(p, [&](auto r) { return decltype(r)::init(p, b, s); });
+}
+
+int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                     void* stream) {
+  int st = validate(p, b);
+  if (st) return st;
+  if (iters < 0) return OPYX_ERR_ARG;
+  if (iters == 0) return OPYX_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch(p, [&](auto r) { return decltype(r)::iterate(p, b, iters, s); });
+}
+
+int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
+                  void* stream) {
+  int st = validate(p, b);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch(p, [&](auto r) { return decltype(r)::pass(p, b, which, s); });
+}
+
+int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream) {
+  int st = validate(p, b);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch(p, [&](auto r) { return decltype(r)::gap(p, b, s); });
+}
+
+}  // extern "C"

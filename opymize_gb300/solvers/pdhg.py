@@ -1,0 +1,406 @@
+"""PDHG (Chambolle-Pock) solver on the GPU (opymize/solvers/pdhg.py).
+
+``PDHG(g, f, A).solve(...)`` keeps the reference's keyword set and ``info``
+dictionary.  Two device paths:
+
+* fused -- G = SSD, F = L1Norms (Frobenius) or HuberL1Norms, A = forward
+  GradientOp with D <= 3 and C <= 4: every iteration is two fused passes
+  (three with adaptive steps) from libopyx, ``granularity`` iterations plus the
+  FP64 gap are captured into one CUDA graph and replayed, and the host reads a
+  104-byte info record once per check;
+* generic -- any composition of GPU operators and functionals: the
+  reference's iteration with the step kernels of libopyx, adaptive steps
+  updated on the device, the gap from FP64 device reductions.
+
+``use_gpu=False`` is refused: this package has no CPU path.
+"""
+
+import logging
+import time
+
+import numpy as np
+
+from opymize_gb300 import _lib
+from opymize_gb300.gpuarray import DeviceArray, stream_ptr, torch
+from opymize_gb300.steps import DeviceScalar, step_struct
+from opymize_gb300.linear import normest
+from opymize_gb300.linear.diff import GradientOp
+from opymize_gb300.functionals.quad import SSD
+from opymize_gb300.functionals.l1norms import L1Norms, HuberL1Norms
+from opymize_gb300.tools import truncate
+from opymize_gb300.tools.util import GracefulInterruptHandler
+
+INFO_KEYS = ("objp", "objd", "infeasp", "infeasd", "gap", "relgap")
+
+
+class PDHG(object):
+    def __init__(self, g, f, A):
+        assert A.x.size == g.x.size
+        assert A.y.size == f.x.size
+        self.g = g
+        self.f = f
+        self.linop = A
+        self.itervars = {}
+        self.constvars = {}
+        self.use_gpu = True
+        self.info = {}
+        self.path = None
+
+    # ------------------------------------------------------------------ API
+    def solve(self, continue_at=None, precision="double", steps="const", step_bound=None,
+              step_factor=1.0, term_pd_gap=1e-5, term_pd_res=None, term_maxiter=int(5e4),
+              granularity=5000, use_gpu=True, cbfun=None, fused=None, graph=True):
+        """Solve to the termination criteria of the reference
+        (opymize/solvers/pdhg.py:229-315) on the GPU.
+
+        Extra keywords: ``fused`` (None = automatic, False forces the generic
+        path) and ``graph`` (capture chunks of the fused path in CUDA graphs).
+        """
+        if not use_gpu:
+            raise NotImplementedError("opymize_gb300 has no CPU path: use_gpu must be True")
+        if steps == "constant":
+            steps = "const"
+        if steps not in ("const", "adaptive", "precond"):
+            raise ValueError("unknown steps rule: %s" % steps)
+        dtype = np.float64 if precision == "double" else np.float32
+        i, c = self.itervars, self.constvars
+        i.clear()
+        c.clear()
+        self.info = {}
+        i['xk'] = self.g.x.new(dtype=dtype)
+        i['yk'] = self.f.x.new(dtype=dtype)
+        if continue_at is not None:
+            i['xk'][:], i['yk'][:] = continue_at
+        if term_maxiter == 0:
+            self.info['iter'] = 0
+            return self.info
+
+        pd_res_mode = term_pd_res is not None
+        if pd_res_mode:
+            steps = "adaptive"
+            if type(term_pd_res) is not tuple:
+                term_pd_res = (term_pd_res,) * 4
+            else:
+                assert len(term_pd_res) == 4
+            self.info['epspd'] = term_pd_res
+        else:
+            if type(term_pd_gap) is not tuple:
+                term_pd_gap = (term_pd_gap, term_pd_gap)
+            if steps == "adaptive":
+                self.info['epspd'] = (term_pd_gap[0],) * 4
+        c['theta'] = 1.0
+
+        bnd = None
+        if steps != "precond":
+            bnd = step_bound
+            if step_bound is None:
+                logging.info("Estimating optimal step bound...")
+                op_norm, itn = normest(self.linop)
+                bnd = truncate(1.0 / op_norm ** 2, 3)
+        self.step_bound = bnd
+        if steps == "adaptive":
+            c['adaptive'] = True
+            c['eta'], c['Delta'] = 0.95, 1.50
+            i['alphak'] = 0.5
+            i['sigmak'] = i['tauk'] = np.sqrt(bnd)
+        elif steps == "const":
+            c['sigma'] = np.sqrt(bnd / step_factor)
+            c['tau'] = bnd / c['sigma']
+        else:
+            c['precond'] = True
+
+        use_fused = self._fusable() if fused is None else (fused and self._fusable())
+        self.path = "fused" if use_fused else "generic"
+        args = (dtype, steps, term_pd_gap, term_pd_res, pd_res_mode, term_maxiter,
+                granularity, cbfun)
+        if use_fused:
+            self._solve_fused(*args, graph=graph)
+        else:
+            self._solve_generic(*args)
+        return self.info
+
+    @property
+    def state(self):
+        return (self.itervars['xk'], self.itervars['yk'])
+
+    # ------------------------------------------------------------ helpers
+    def _fusable(self):
+        g, f, A = self.g, self.f, self.linop
+        if type(g) is not SSD or type(A) is not GradientOp or A.scheme != "forward":
+            return False
+        D, C = len(A.imagedims), A.nchannels
+        if D > 3 or C > _lib.ROF_MAX_C:
+            return False
+        if type(f) is L1Norms:
+            if f.matrixnorm != "frobenius" and min(f.M) > 1:
+                return False
+        elif type(f) is not HuberL1Norms:
+            return False
+        return f.N == int(np.prod(A.imagedims)) and f.M[0] * f.M[1] == D * C
+
+    def _check(self, pd_res_mode, term_pd_gap):
+        if pd_res_mode:
+            return self.info['resp'] < self.info['epsp'] and self.info['resd'] < self.info['epsd']
+        test_err = np.abs(self.info['relgap']) < term_pd_gap[0]
+        test_infeas = max(self.info['infeasp'], self.info['infeasd']) < term_pd_gap[1]
+        return test_err and test_infeas
+
+    # ------------------------------------------------------------ fused
+    def _rof_problem(self, dtype, steps):
+        g, f, A = self.g, self.f, self.linop
+        c, i = self.constvars, self.itervars
+        p = _lib.opyx_rof_problem()
+        p.dtype = _lib.OPYX_F32 if dtype == np.float32 else _lib.OPYX_F64
+        D, C = len(A.imagedims), A.nchannels
+        p.ndim, p.nchannels, p.steps = D, C, _lib.STEPS[steps]
+        for t in range(D):
+            p.dims[t] = A.imagedims[t]
+            p.h[t] = float(A.imageh[t])
+        for k in range(C):
+            p.weights[k] = float(A.weights[k])
+            p.vol[k] = float(g.vol[k])
+        p.ssd_shift = float(g.shift)
+        p.lbd = float(f.lbd)
+        p.huber_alpha = float(f.alph) if isinstance(f, HuberL1Norms) else 0.0
+        p.theta = float(c['theta'])
+        if steps == "const":
+            p.tau, p.sigma = float(c['tau']), float(c['sigma'])
+        elif steps == "adaptive":
+            p.tau, p.sigma = float(i['tauk']), float(i['sigmak'])
+            p.alpha0, p.eta, p.Delta = float(i['alphak']), float(c['eta']), float(c['Delta'])
+            for j in range(4):
+                p.eps[j] = float(self.info['epspd'][j])
+        return p
+
+    def _solve_fused(self, dtype, steps, term_pd_gap, term_pd_res, pd_res_mode, term_maxiter,
+                     granularity, cbfun, graph=True):
+        lib = _lib.load()
+        i = self.itervars
+        A = self.linop
+        N, C, D = int(np.prod(A.imagedims)), A.nchannels, len(A.imagedims)
+        x = DeviceArray.to_gpu(i['xk'], dtype)
+        y = DeviceArray.to_gpu(i['yk'], dtype)
+        xbar = DeviceArray.empty((N * C,), dtype)
+        fdev = self.g.f_dev(dtype)
+        mask = self.g.mask_dev()
+        adaptive = steps == "adaptive"
+        xgrad = DeviceArray.empty((N * C,), dtype) if adaptive else None
+        gp = DeviceArray.empty((N * C,), dtype) if adaptive else None
+        wsb = lib.opyx_rof_workspace_size()
+        ws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
+        p = self._rof_problem(dtype, steps)
+        b = _lib.opyx_rof_buffers()
+        b.x, b.xbar, b.y, b.f = x.ptr, xbar.ptr, y.ptr, fdev.ptr
+        b.mask = None if mask is None else mask.ptr
+        b.xgrad = None if xgrad is None else xgrad.ptr
+        b.gp = None if gp is None else gp.ptr
+        b.ws = ws.ptr
+        self._fused = dict(x=x, y=y, xbar=xbar, f=fdev, mask=mask, xgrad=xgrad, gp=gp, ws=ws,
+                           problem=p, buffers=b)
+        info_off = lib.opyx_rof_info_offset() // 8
+        s = stream_ptr()
+        _lib.call("opyx_rof_init", p, b, s)
+
+        graphs = {}
+
+        def run_chunk(n):
+            if graph:
+                if n not in graphs:
+                    graphs[n] = _RofGraph(p, b, n)
+                graphs[n].launch()
+            else:
+                _lib.call("opyx_rof_iterate", p, b, n, stream_ptr())
+                _lib.call("opyx_rof_gap", p, b, stream_ptr())
+
+        t0 = time.perf_counter()
+        _iter = 0
+        with GracefulInterruptHandler() as hdl:
+            while _iter < term_maxiter:
+                n = min(granularity - (_iter % granularity), term_maxiter - _iter)
+                check = (_iter + n) % granularity == 0
+                if check:
+                    run_chunk(n)
+                else:
+                    _lib.call("opyx_rof_iterate", p, b, n, stream_ptr())
+                _iter += n
+                if hdl.interrupted or check:
+                    if not check:
+                        _lib.call("opyx_rof_gap", p, b, stream_ptr())
+                    rec = ws[info_off:info_off + 13].get()
+                    self._record_info(rec, _iter, t0)
+                    if cbfun is not None:
+                        self._download(x, y)
+                        cbfun(self.state, self.info)
+                    if self._check(pd_res_mode, term_pd_gap) or hdl.interrupted:
+                        break
+        self._download(x, y)
+        self.info.setdefault('iter', _iter)
+        self.info['iter'] = _iter
+
+    def _record_info(self, rec, it, t0):
+        names = ("objp", "objd", "infeasp", "infeasd", "gap", "relgap", "tau", "sigma",
+                 "alpha", "resp", "resd", "epsp", "epsd")
+        d = dict(zip(names, (float(v) for v in rec)))
+        for k in INFO_KEYS:
+            self.info[k] = d[k]
+        if 'adaptive' in self.constvars:
+            self.itervars['tauk'], self.itervars['sigmak'] = d['tau'], d['sigma']
+            self.itervars['alphak'] = d['alpha']
+            for k in ("resp", "resd", "epsp", "epsd"):
+                self.info[k] = d[k]
+        self.info['iter'] = it
+        el = time.perf_counter() - t0
+        self.info['time_s'] = el
+        self.info['it_per_s'] = it / el if el > 0 else float('inf')
+
+    def _download(self, x, y):
+        self.itervars['xk'] = x.get().reshape(self.itervars['xk'].shape)
+        self.itervars['yk'] = y.get().reshape(self.itervars['yk'].shape)
+
+    # ------------------------------------------------------------ generic
+    def _solve_generic(self, dtype, steps, term_pd_gap, term_pd_res, pd_res_mode,
+                       term_maxiter, granularity, cbfun):
+        i, c = self.itervars, self.constvars
+        v = {}
+        v['xk'] = DeviceArray.to_gpu(i['xk'], dtype)
+        v['yk'] = DeviceArray.to_gpu(i['yk'], dtype)
+        for s_ in ('xkp1', 'xgradk', 'xgradkp1'):
+            v[s_] = DeviceArray.empty((self.g.x.size,), dtype)
+        for s_ in ('ykp1', 'ygradk', 'ygradkp1'):
+            v[s_] = DeviceArray.empty((self.f.x.size,), dtype)
+        self.linop(v['xk'], v['ygradk'])
+        self.linop.adjoint(v['yk'], v['xgradk'])
+        self.gpu_itervars = v
+        st = None
+        if steps == "precond":
+            c['xtau'] = DeviceArray.empty((self.g.x.size,), dtype)
+            c['ysigma'] = DeviceArray.empty((self.f.x.size,), dtype)
+            self.linop.rowwise_lp(c['ysigma'])
+            self.linop.adjoint.rowwise_lp(c['xtau'])
+            _invert_positive(c['ysigma'])
+            _invert_positive(c['xtau'])
+            tau, sigma = c['xtau'], c['ysigma']
+        elif steps == "adaptive":
+            st = _AdaptiveState(i['tauk'], i['sigmak'], i['alphak'], c['eta'], c['Delta'],
+                                c['theta'], self.info['epspd'], self.g.x.size, self.f.x.size)
+            tau, sigma = st.tau, st.sigma
+            self._adaptive = st
+        else:
+            tau, sigma = c['tau'], c['sigma']
+        gprox = self.g.prox(tau)
+        fconjprox = self.f.conj.prox(sigma)
+        ws = DeviceArray.zeros(((_lib.load().opyx_reduce_workspace_size() + 7) // 8,),
+                               np.float64)
+        theta = c['theta']
+        t0 = time.perf_counter()
+        _iter = 0
+        with GracefulInterruptHandler() as hdl:
+            while _iter < term_maxiter:
+                _iter += 1
+                check = (_iter % granularity == 0)
+                s = stream_ptr()
+                _lib.call("opyx_take_step", v['xk'].dcode, v['xk'].size, v['xkp1'].ptr,
+                          v['xk'].ptr, -1, step_struct(tau, dtype), v['xgradk'].ptr, s)
+                gprox(v['xkp1'])
+                self.linop(v['xkp1'], v['ygradkp1'])
+                _lib.call("opyx_dual_step", v['yk'].dcode, v['yk'].size, v['ykp1'].ptr,
+                          v['yk'].ptr, step_struct(sigma, dtype), theta, v['ygradkp1'].ptr,
+                          v['ygradk'].ptr, s)
+                fconjprox(v['ykp1'])
+                self.linop.adjoint(v['ykp1'], v['xgradkp1'])
+                if st is not None:
+                    _lib.call("opyx_residual_pair", v['xk'].dcode, v['xk'].size,
+                              step_struct(st.tau), v['xk'].ptr, v['xkp1'].ptr, 1.0,
+                              v['xgradk'].ptr, 1.0, 0.0, v['xgradkp1'].ptr, st.sums_ptr(0),
+                              ws.ptr, s)
+                    _lib.call("opyx_residual_pair", v['yk'].dcode, v['yk'].size,
+                              step_struct(st.sigma), v['yk'].ptr, v['ykp1'].ptr, theta,
+                              v['ygradk'].ptr, theta, theta + 1.0, v['ygradkp1'].ptr,
+                              st.sums_ptr(2), ws.ptr, s)
+                    _lib.call("opyx_adaptive_update", st.ptr, s)
+                for a_, b_ in (('xk', 'xkp1'), ('xgradk', 'xgradkp1'), ('yk', 'ykp1'),
+                               ('ygradk', 'ygradkp1')):
+                    v[a_], v[b_] = v[b_], v[a_]
+                if hdl.interrupted or check:
+                    self.info['iter'] = _iter
+                    if st is not None:
+                        h = st.read()
+                        i['tauk'], i['sigmak'], i['alphak'] = h.tau, h.sigma, h.alpha
+                        self.info.update(resp=h.resp, resd=h.resd, epsp=h.epsp, epsd=h.epsd)
+                    if not pd_res_mode:
+                        self.info.update(self.pd_gap())
+                    el = time.perf_counter() - t0
+                    self.info['time_s'], self.info['it_per_s'] = el, _iter / el
+                    if cbfun is not None:
+                        self._download(v['xk'], v['yk'])
+                        cbfun(self.state, self.info)
+                    if self._check(pd_res_mode, term_pd_gap) or hdl.interrupted:
+                        break
+        self._download(v['xk'], v['yk'])
+        self.info['iter'] = _iter
+
+    def pd_gap(self):
+        """Primal-dual gap of the current device iterate (pdhg.py:23-44),
+        every functional reduced in FP64 on the device."""
+        v = self.gpu_itervars
+        obj, inf1 = self.g(v['xk'])
+        obj2, inf2 = self.f(v['ygradk'])
+        objp, infeasp = obj + obj2, inf1 + inf2
+        neg = v['xgradk'].copy()
+        neg *= -1.0
+        obj, inf1 = self.g.conj(neg)
+        obj2, inf2 = self.f.conj(v['yk'])
+        objd, infeasd = -obj - obj2, inf1 + inf2
+        return {'objp': objp, 'objd': objd, 'infeasp': infeasp, 'infeasd': infeasd,
+                'gap': objp - objd,
+                'relgap': (objp - objd) / max(np.spacing(1), abs(objd))}
+
+
+def _invert_positive(a):
+    """a_i <- 1/a_i where a_i > eps, else unchanged (pdhg.py:197-198)."""
+    _lib.call("opyx_recip_positive", a.dcode, a.size, a.ptr, float(np.spacing(1)), stream_ptr())
+
+
+class _AdaptiveState(object):
+    """Device record of the adaptive rule (opyx_adaptive_state)."""
+
+    def __init__(self, tau, sigma, alpha, eta, Delta, theta, eps, xsize, ysize):
+        h = _lib.opyx_adaptive_state()
+        h.tau, h.sigma, h.alpha, h.eta, h.Delta, h.theta = tau, sigma, alpha, eta, Delta, theta
+        for j in range(4):
+            h.eps[j] = eps[j]
+        h.xsize, h.ysize = float(xsize), float(ysize)
+        raw = np.frombuffer(bytes(h), dtype=np.float64).copy()
+        self.dev = DeviceArray.to_gpu(raw)
+        self.ptr = self.dev.ptr
+        self.tau = DeviceScalar(self.ptr + _lib.opyx_adaptive_state.tau.offset, self.dev, tau)
+        self.sigma = DeviceScalar(self.ptr + _lib.opyx_adaptive_state.sigma.offset, self.dev,
+                                  sigma)
+
+    def sums_ptr(self, j):
+        return self.ptr + _lib.opyx_adaptive_state.sums.offset + 8 * j
+
+    def read(self):
+        raw = self.dev.get()
+        h = _lib.opyx_adaptive_state.from_buffer_copy(raw.tobytes())
+        self.tau.host_value, self.sigma.host_value = h.tau, h.sigma
+        return h
+
+
+class _RofGraph(object):
+    """`n` fused iterations followed by the gap kernel, captured once into a
+    CUDA graph (on a private capture stream) and replayed on the current
+    stream."""
+
+    def __init__(self, p, b, n):
+        t = torch()
+        self.stream = t.cuda.Stream()
+        self.graph = t.cuda.CUDAGraph()
+        self.stream.wait_stream(t.cuda.current_stream())
+        with t.cuda.graph(self.graph, stream=self.stream):
+            s = t.cuda.current_stream().cuda_stream
+            _lib.call("opyx_rof_iterate", p, b, n, s)
+            _lib.call("opyx_rof_gap", p, b, s)
+
+    def launch(self):
+        self.graph.replay()

@@ -1,0 +1,153 @@
+"""GPU solver parity: PDHG iterates and duality gaps against the reference's
+own CPU PDHG (fixtures in tests/golden/ made by running the reference) and
+against the CPU oracle.
+
+Bars (from the PDHG path's spec): relative L2 error of x and y <= 1e-12 in
+FP64 mode and <= 1e-5 in FP32 mode after a fixed iteration count."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import GOLDEN
+from tests.test_oracle import build_problem
+
+pytestmark = pytest.mark.gpu
+
+SOLVER_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN)
+                      if f.endswith(".npz") and f != "ops.npz")
+SMALL_CASES = [c for c in SOLVER_CASES if c != "rof_gray256_adaptive"]
+
+
+def gpu_problem(d):
+    from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    dims = tuple(int(v) for v in d["imagedims"])
+    f = d["f"]
+    C, D, N = f.shape[-1], len(dims), int(np.prod(dims))
+    G = SSD(f.reshape(N, C), vol=d["vol"], mask=d["mask"])
+    if float(d["huber"]) > 0:
+        F = HuberL1Norms(N, (C, D), float(d["lbd"]), float(d["huber"]))
+    else:
+        F = L1Norms(N, (C, D), float(d["lbd"]))
+    A = GradientOp(dims, C, scheme=str(d["scheme"]), imageh=d["imageh"], weights=d["weights"])
+    return G, F, A
+
+
+def run_gpu(d, precision, fused=None, iters=None, graph=True):
+    from opymize_gb300.solvers import PDHG
+    G, F, A = gpu_problem(d)
+    solver = PDHG(G, F, A)
+    rec = {}
+
+    def cb(state, info):
+        rec[info["iter"]] = (state[0].copy(), state[1].copy(), dict(info),
+                             solver.itervars.get("tauk", np.nan))
+
+    np.random.seed(0)
+    solver.solve(steps=str(d["steps"]), precision=precision, term_pd_gap=1e-300,
+                 term_maxiter=int(d["iters_total"]) if iters is None else iters,
+                 granularity=int(d["gran"]), cbfun=cb, fused=fused, graph=graph)
+    return solver, rec
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a, np.float64) - b) / max(1e-300, np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("fused", [True, False])
+@pytest.mark.parametrize("case", SMALL_CASES)
+def test_fp64_matches_reference(case, fused):
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    solver, rec = run_gpu(d, "double", fused=fused)
+    if fused and str(d["scheme"]) == "forward":
+        assert solver.path == "fused"
+    else:
+        assert solver.path == "generic"
+    for j, it in enumerate(d["dump_iters"]):
+        x, y, info, tau = rec[int(it)]
+        assert rel(x, d["x"][j]) <= 1e-12, (case, it, rel(x, d["x"][j]))
+        assert rel(y, d["y"][j]) <= 1e-12, (case, it, rel(y, d["y"][j]))
+    for j, it in enumerate(d["info_iters"]):
+        info = rec[int(it)][2]
+        for k in ("objp", "objd", "gap"):
+            ref = d["info_" + k][j]
+            assert abs(info[k] - ref) <= 1e-10 * max(1.0, abs(ref)), (case, k, it, info[k], ref)
+        if str(d["steps"]) == "adaptive":
+            assert abs(rec[int(it)][3] - d["info_tau"][j]) <= 1e-12 * d["info_tau"][j]
+
+
+@pytest.mark.parametrize("case", ["g2d_const_fwd", "g2d_precond_fwd", "c2d_precond_fwd",
+                                  "c2d_huber_precond", "v3d_precond_fwd", "c2d_volmask_const",
+                                  "g1d_precond_fwd", "g2d_const_imageh"])
+def test_fp32_matches_reference(case):
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    solver, rec = run_gpu(d, "float")
+    assert solver.path == "fused"
+    for j, it in enumerate(d["dump_iters"]):
+        x, y, info, tau = rec[int(it)]
+        assert rel(x, d["x"][j]) <= 1e-5, (case, it, rel(x, d["x"][j]))
+        assert rel(y, d["y"][j]) <= 1e-5, (case, it, rel(y, d["y"][j]))
+
+
+@pytest.mark.parametrize("case", ["g2d_adaptive_fwd", "c2d_huber_adaptive", "v3d_adaptive_fwd"])
+def test_fp32_adaptive_matches_reference(case):
+    """FP32 with adaptive steps: the step sequence branches on residual
+    comparisons, so it must also reproduce the reference's tau sequence."""
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    solver, rec = run_gpu(d, "float")
+    for j, it in enumerate(d["dump_iters"]):
+        x, y, info, tau = rec[int(it)]
+        assert abs(tau - d["info_tau"][j]) <= 1e-6 * d["info_tau"][j], (case, it)
+        assert rel(x, d["x"][j]) <= 1e-5, (case, it, rel(x, d["x"][j]))
+        assert rel(y, d["y"][j]) <= 1e-5, (case, it, rel(y, d["y"][j]))
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("float", 1e-5)])
+def test_rof_gray256_adaptive_1000(precision, tol):
+    """256x256 gray ROF, adaptive steps, 1000 iterations, gap every 50: the
+    reference's CPU PDHG on the same seeded input."""
+    d = np.load(os.path.join(GOLDEN, "rof_gray256_adaptive.npz"))
+    solver, rec = run_gpu(d, precision)
+    assert solver.path == "fused"
+    x, y, info, tau = rec[1000]
+    assert rel(x, d["x"][0]) <= tol, rel(x, d["x"][0])
+    assert rel(y, d["y"][0]) <= tol, rel(y, d["y"][0])
+    gaps = np.array([rec[int(it)][2]["relgap"] for it in d["info_iters"]])
+    assert np.max(np.abs(gaps - d["info_relgap"]) / np.abs(d["info_relgap"])) <= \
+        (1e-9 if precision == "double" else 1e-2)
+
+
+def test_graph_and_eager_agree():
+    d = np.load(os.path.join(GOLDEN, "c2d_huber_adaptive.npz"))
+    _, r1 = run_gpu(d, "double", graph=True)
+    _, r2 = run_gpu(d, "double", graph=False)
+    for it in r1:
+        assert np.array_equal(r1[it][0], r2[it][0]) and np.array_equal(r1[it][1], r2[it][1])
+
+
+def test_fused_matches_oracle_on_large_colour_problem():
+    """A 512x384x3 Huber colour problem (precond steps) for 30 iterations in
+    FP64 against the oracle -- a size where the fused kernels run many blocks
+    and grid-stride loops."""
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.functionals import SSD, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    f = piecewise_constant((512, 384), 3, sigma=0.1, seed=21)
+    N = 512 * 384
+    G, F, A = SSD(f.reshape(N, 3)), HuberL1Norms(N, (3, 2), 0.05, 0.01), \
+        GradientOp((512, 384), 3, scheme="forward")
+    s = PDHG(G, F, A)
+    s.solve(steps="precond", precision="double", term_pd_gap=1e-300, term_maxiter=30,
+            granularity=10)
+    assert s.path == "fused"
+    Go, Fo = oracle.SSD(f.reshape(N, 3)), oracle.HuberL1Norms(N, (3, 2), 0.05, 0.01)
+    Ao = oracle.Gradient((512, 384), 3, "forward")
+    so = oracle.PDHG(Go, Fo, Ao)
+    so.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=30, granularity=10)
+    assert rel(s.state[0], so.state[0]) <= 1e-12
+    assert rel(s.state[1], so.state[1]) <= 1e-12
+    assert abs(s.info["relgap"] - so.info["relgap"]) <= 1e-9 * abs(so.info["relgap"])

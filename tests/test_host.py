@@ -1,0 +1,75 @@
+"""CPU tests of host-side logic: Variable views, step-bound truncation,
+synthetic inputs, SIGINT handling and the solver's path selection."""
+
+import os
+import signal
+
+import numpy as np
+import pytest
+
+import oracle
+from opymize_gb300 import Variable
+from opymize_gb300.tools import truncate
+from opymize_gb300.tools.synthetic import piecewise_constant
+from opymize_gb300.tools.util import GracefulInterruptHandler
+from tests.conftest import GOLDEN
+
+
+def test_variable_views():
+    v = Variable((3, 2), (4,))
+    assert v.size == 10
+    data = np.arange(10.0)
+    a, b = v.vars(data)
+    assert a.shape == (3, 2) and b.shape == (4,)
+    assert b[0] == 6
+    assert v[1]['offset'] == 6
+    named = Variable(('x', (2, 2)), ('y', 3))
+    d = named.vars(np.arange(7.0), named=True)
+    assert d['y'].tolist() == [4.0, 5.0, 6.0]
+
+
+def test_truncate_matches_oracle_and_reference_values():
+    ops = np.load(os.path.join(GOLDEN, "ops.npz"))
+    for x, y in zip(ops["truncate/x"], ops["truncate/y"]):
+        assert truncate(x, 3) == y == oracle.truncate(x, 3)
+
+
+def test_synthetic_generator_is_seeded():
+    a = piecewise_constant((64, 48), 3, seed=7)
+    b = piecewise_constant((64, 48), 3, seed=7)
+    c = piecewise_constant((64, 48), 3, seed=8)
+    assert a.shape == (64, 48, 3)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    v = piecewise_constant((16, 12, 10), 1, seed=1)
+    assert v.shape == (16, 12, 10, 1)
+    # the fixtures were generated by this generator
+    d = np.load(os.path.join(GOLDEN, "g2d_const_fwd.npz"))
+    assert np.array_equal(d["f"], piecewise_constant((32, 24), 1, sigma=0.1, seed=1))
+
+
+def test_salt_and_pepper():
+    img = piecewise_constant((100, 100), 1, sigma=0.0, seed=3, salt_pepper=0.1)
+    frac = np.mean((img == 0.0) | (img == 1.0))
+    assert 0.05 < frac < 0.5
+
+
+def test_graceful_interrupt():
+    with GracefulInterruptHandler() as h:
+        os.kill(os.getpid(), signal.SIGINT)
+        assert h.interrupted
+    assert signal.getsignal(signal.SIGINT) is not None
+
+
+def test_fused_path_selection():
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms, QuadEpiInd
+    from opymize_gb300.linear import GradientOp, LaplacianOp
+    f = np.zeros((20, 1))
+    fwd = GradientOp((4, 5), 1, scheme="forward")
+    cen = GradientOp((4, 5), 1, scheme="centered")
+    assert PDHG(SSD(f), L1Norms(20, (1, 2), 0.1), fwd)._fusable()
+    assert PDHG(SSD(f), HuberL1Norms(20, (1, 2), 0.1, 0.01), fwd)._fusable()
+    assert not PDHG(SSD(f), L1Norms(20, (1, 2), 0.1), cen)._fusable()
+    lap = LaplacianOp((4, 5), 1)
+    assert not PDHG(SSD(f), SSD(np.zeros((20, 1))), lap)._fusable()
+    assert not PDHG(SSD(f), QuadEpiInd(20, 1), GradientOp((4, 5), 1, "forward"))._fusable()
