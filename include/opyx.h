@@ -57,6 +57,9 @@ int opyx_axpby(int dtype, int64_t n, double a, const void* x, double b, void* y,
 /* y = |x| elementwise (numpy `np.abs`, power iteration of normest:
  * opymize/linear/__init__.py:11-46). */
 int opyx_abs(int dtype, int64_t n, const void* x, void* y, void* stream);
+/* y = x converted between OPYX_F64 and OPYX_F32 (uploads of FP64 host data
+ * for FP32 iterates are converted on the device). */
+int opyx_cast(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, void* stream);
 /* x_i <- 1/x_i where x_i > eps, unchanged elsewhere: the diagonal
  * preconditioners from rowwise norms (opymize/solvers/pdhg.py:197-198). */
 int opyx_recip_positive(int dtype, int64_t n, void* x, double eps, void* stream);

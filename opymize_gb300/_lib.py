@@ -99,6 +99,7 @@ SIGNATURES = {
     "opyx_axpby": (i32, [i32, i64, f64, vp, f64, vp, vp]),
     "opyx_abs": (i32, [i32, i64, vp, vp, vp]),
     "opyx_recip_positive": (i32, [i32, i64, vp, f64, vp]),
+    "opyx_cast": (i32, [i32, i32, i64, vp, vp, vp]),
     "opyx_broadcast_mid": (i32, [i32, vp, i64, i64, i64, vp, i32, vp]),
     "opyx_reduce_workspace_size": (sz, []),
     "opyx_norms": (i32, [i32, i64, vp, vp, vp, vp]),

@@ -44,23 +44,47 @@ static int validate(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   return OPYX_OK;
 }
 
-static Geo make_geo(const opyx_rof_problem* p) {
-  Geo g;
+template <typename T>
+static Geo<T> make_geo(const opyx_rof_problem* p) {
+  Geo<T> g;
+  memset(&g, 0, sizeof(g));
   const int D = p->ndim;
+  double invh[3] = {1.0, 1.0, 1.0};
   g.N = 1;
-  for (int t = 0; t < 3; ++t) { g.n[t] = 1; g.s[t] = 1; g.invh[t] = 1.0; }
-  for (int t = 0; t < D; ++t) { g.n[t] = p->dims[t]; g.invh[t] = 1.0 / p->h[t]; g.N *= p->dims[t]; }
+  for (int t = 0; t < 3; ++t) { g.n[t] = 1; g.s[t] = 1; }
+  for (int t = 0; t < D; ++t) { g.n[t] = p->dims[t]; invh[t] = 1.0 / p->h[t]; g.N *= p->dims[t]; }
   int64_t s = 1;
   for (int t = D - 1; t >= 0; --t) { g.s[t] = s; s *= g.n[t]; }
   g.nl = g.n[D - 1];
   g.rows = g.N / g.nl;
-  for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
-    g.w[k] = k < p->nchannels ? p->weights[k] : 1.0;
-    g.vol[k] = k < p->nchannels ? p->vol[k] : 1.0;
+  for (int t = 0; t < 3; ++t) {
+    g.invh[t] = (T)invh[t];
+    for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
+      const double w = k < p->nchannels ? p->weights[k] : 1.0;
+      g.coef[t][k] = (T)(w * invh[t]);
+      g.absc[t][k] = (T)(fabs(w) * invh[t]);
+      const double rs = 2.0 * fabs(w) * invh[t];
+      g.sig_pre[t][k] = (T)(rs > 2.220446049250313e-16 ? 1.0 / rs : 0.0);
+    }
   }
-  g.lbd = p->lbd;
-  g.huber = p->huber_alpha;
-  g.theta = p->theta;
+  for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
+    const double w = k < p->nchannels ? p->weights[k] : 1.0;
+    const double v = k < p->nchannels ? p->vol[k] : 1.0;
+    g.w[k] = (T)w;
+    g.vol[k] = (T)v;
+    g.half_rvol[k] = (T)(0.5 / v);
+  }
+  g.lbd = (T)p->lbd;
+  g.lbd2 = (T)(p->lbd * p->lbd);
+  g.lbd_d = p->lbd;
+  g.huber_d = p->huber_alpha;
+  g.use_huber = p->huber_alpha > 0;
+  g.huber = (T)p->huber_alpha;
+  g.half_huber = (T)(0.5 * p->huber_alpha);
+  g.half_rhuber = (T)(p->huber_alpha > 0 ? 0.5 / p->huber_alpha : 0.0);
+  g.hub_ratio = (T)(p->huber_alpha / p->lbd);
+  g.theta = (T)p->theta;
+  g.theta1 = (T)(1.0 + p->theta);
   g.steps = p->steps;
   return g;
 }
@@ -88,7 +112,8 @@ static Args<T> make_args(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
 // Launch shape: 32 x 8 threads; x covers the contiguous axis, y-blocks run
 // grid-stride over the remaining rows.  Reduction kernels cap the number of
 // blocks at kMaxBlocks (their partials buffer).
-static void shape(const Geo& g, dim3* grid, dim3* block, bool reduce) {
+template <typename T>
+static void shape(const Geo<T>& g, dim3* grid, dim3* block, bool reduce) {
   *block = dim3(32, 8, 1);
   const int64_t cap_total = reduce ? kMaxBlocks : (int64_t)sm_count() * 64;
   int64_t gx = (g.nl + 31) / 32;
@@ -104,7 +129,7 @@ static void shape(const Geo& g, dim3* grid, dim3* block, bool reduce) {
 template <typename T, int D, int C>
 struct Runner {
   static int init(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
-    Geo g = make_geo(p);
+    Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
     if (p->steps == OPYX_STEPS_ADAPTIVE) {
       dim3 grid, block;
@@ -117,7 +142,7 @@ struct Runner {
 
   static int iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
                      cudaStream_t s) {
-    Geo g = make_geo(p);
+    Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
     dim3 grid, block, rgrid, rblock;
     shape(g, &grid, &block, false);
@@ -137,7 +162,7 @@ struct Runner {
 
   static int pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   cudaStream_t s) {
-    Geo g = make_geo(p);
+    Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
     dim3 grid, block, rgrid, rblock;
     shape(g, &grid, &block, false);
@@ -158,7 +183,7 @@ struct Runner {
   }
 
   static int gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
-    Geo g = make_geo(p);
+    Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
     dim3 grid, block;
     shape(g, &grid, &block, true);

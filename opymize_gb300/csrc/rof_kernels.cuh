@@ -28,17 +28,28 @@
 namespace opyx {
 namespace rof {
 
+// Problem geometry and coefficients.  Everything a kernel touches per pixel
+// is precomputed on the host in the iterate type T, so FP32 kernels do no
+// FP64 arithmetic outside the gap reductions.
+template <typename T>
 struct Geo {
   int64_t N;          // pixels
   int64_t nl;         // length of the last (contiguous) axis
   int64_t rows;       // N / nl
   int64_t n[3];       // dims (n[0..D-1])
   int64_t s[3];       // strides in pixels
-  double invh[3];
-  double w[OPYX_ROF_MAX_C];
-  double vol[OPYX_ROF_MAX_C];
-  double lbd, huber, theta;
+  T invh[3];                          // 1/h_t
+  T coef[3][OPYX_ROF_MAX_C];          // w_k/h_t
+  T absc[3][OPYX_ROF_MAX_C];          // |w_k|/h_t (preconditioner sums)
+  T sig_pre[3][OPYX_ROF_MAX_C];       // h_t/(2|w_k|): sigma of inner rows
+  T w[OPYX_ROF_MAX_C];
+  T vol[OPYX_ROF_MAX_C];
+  T half_rvol[OPYX_ROF_MAX_C];        // 1/(2 vol_k)
+  T lbd, lbd2, hub_ratio, theta, theta1;
+  T huber, half_huber, half_rhuber;   // alpha, alpha/2, 1/(2 alpha)
+  double lbd_d, huber_d;
   int steps;
+  bool use_huber;
 };
 
 // Per-launch constants, by value.
@@ -59,8 +70,8 @@ struct Args {
 };
 
 // Coordinates of pixel (row r, column q): c[D-1] = q, the others from r.
-template <int D>
-OPYX_D void coords(const Geo& g, int64_t r, int64_t q, int64_t* c) {
+template <typename T, int D>
+OPYX_D void coords(const Geo<T>& g, int64_t r, int64_t q, int64_t* c) {
   c[D - 1] = q;
   if (D == 2) c[0] = r;
   if (D == 3) { c[1] = r % g.n[1]; c[0] = r / g.n[1]; }
@@ -69,33 +80,31 @@ OPYX_D void coords(const Geo& g, int64_t r, int64_t q, int64_t* c) {
 // Analytic diagonal preconditioners of the forward gradient
 // (pdhg.py:191-204 with the rowwise l1 norms of diffopn):
 //   sigma_{i,t,k} = 1/(2|w_k|/h_t) on inner rows, 0 on the far boundary;
-//   tau_{i,k}     = 1/(|w_k| sum_t ([c_t < n_t-1] + [c_t > 0]) / h_t).
-template <int D>
-OPYX_D double precond_sigma(const Geo& g, const int64_t* c, int t, int k) {
-  if (c[t] >= g.n[t] - 1) return 0.0;
-  const double rs = 2.0 * fabs(g.w[k]) * g.invh[t];
-  return rs > 2.220446049250313e-16 ? 1.0 / rs : 0.0;
+//   tau_{i,k}     = 1/(sum_t |w_k|/h_t ([c_t < n_t-1] + [c_t > 0])).
+template <typename T, int D>
+OPYX_D T precond_sigma(const Geo<T>& g, const int64_t* c, int t, int k) {
+  return c[t] < g.n[t] - 1 ? g.sig_pre[t][k] : T(0);
 }
 
-template <int D>
-OPYX_D double precond_tau(const Geo& g, const int64_t* c, int k) {
-  double cs = 0.0;
+template <typename T, int D>
+OPYX_D T precond_tau(const Geo<T>& g, const int64_t* c, int k) {
+  T cs = T(0);
 #pragma unroll
   for (int t = 0; t < D; ++t)
-    cs += fabs(g.w[k]) * g.invh[t] * (double)((c[t] < g.n[t] - 1) + (c[t] > 0));
-  return cs > 2.220446049250313e-16 ? 1.0 / cs : 0.0;
+    cs += g.absc[t][k] * (T)((c[t] < g.n[t] - 1) + (c[t] > 0));
+  return cs > T(2.220446049250313e-16) ? T(1) / cs : T(0);
 }
 
 // (A^T y)_i = w_k * sum_t (-y[i,t,k]/h_t [c_t < n_t-1] + y[i-s_t,t,k]/h_t [c_t > 0])
 // (divergence, diff.cu:114-123).
 template <typename T, int D, int C>
-OPYX_D void div_at(const Geo& g, const T* __restrict__ y, int64_t i, const int64_t* c,
+OPYX_D void div_at(const Geo<T>& g, const T* __restrict__ y, int64_t i, const int64_t* c,
                    T (&out)[C]) {
 #pragma unroll
   for (int k = 0; k < C; ++k) out[k] = T(0);
 #pragma unroll
   for (int t = 0; t < D; ++t) {
-    const T ih = (T)g.invh[t];
+    const T ih = g.invh[t];
     if (c[t] < g.n[t] - 1) {
 #pragma unroll
       for (int k = 0; k < C; ++k) out[k] -= y[(i * D + t) * C + k] * ih;
@@ -107,13 +116,13 @@ OPYX_D void div_at(const Geo& g, const T* __restrict__ y, int64_t i, const int64
     }
   }
 #pragma unroll
-  for (int k = 0; k < C; ++k) out[k] *= (T)g.w[k];
+  for (int k = 0; k < C; ++k) out[k] *= g.w[k];
 }
 
 // (A v)_{i,t,k} = w_k/h_t (v[i+s_t,k] - v[i,k]) if c_t < n_t-1 else 0
 // (gradient, diff.cu:64-74).
 template <typename T, int D, int C>
-OPYX_D void grad_at(const Geo& g, const T* __restrict__ v, int64_t i, const int64_t* c,
+OPYX_D void grad_at(const Geo<T>& g, const T* __restrict__ v, int64_t i, const int64_t* c,
                     T (&out)[D * C]) {
   T vi[C];
 #pragma unroll
@@ -123,7 +132,7 @@ OPYX_D void grad_at(const Geo& g, const T* __restrict__ v, int64_t i, const int6
     if (c[t] < g.n[t] - 1) {
       const int64_t j = i + g.s[t];
 #pragma unroll
-      for (int k = 0; k < C; ++k) out[t * C + k] = (T)(g.w[k] * g.invh[t]) * (v[j * C + k] - vi[k]);
+      for (int k = 0; k < C; ++k) out[t * C + k] = g.coef[t][k] * (v[j * C + k] - vi[k]);
     } else {
 #pragma unroll
       for (int k = 0; k < C; ++k) out[t * C + k] = T(0);
@@ -134,20 +143,27 @@ OPYX_D void grad_at(const Geo& g, const T* __restrict__ v, int64_t i, const int6
 // prox of sigma*F*: optional Huber shrink y/(1 + sigma*alpha/lbd), then the
 // projection of the D*C group onto the Frobenius ball of radius lbd.
 template <typename T, int M>
-OPYX_D void fconj_prox(const Geo& g, T (&yv)[M], const T (&sig)[M]) {
-  if (g.huber > 0) {
+OPYX_D void fconj_prox(const Geo<T>& g, T (&yv)[M], const T (&sig)[M]) {
+  if (g.use_huber) {
 #pragma unroll
-    for (int j = 0; j < M; ++j) yv[j] /= T(1) + sig[j] * (T)(g.huber / g.lbd);
+    for (int j = 0; j < M; ++j) yv[j] /= T(1) + sig[j] * g.hub_ratio;
   }
-  frob_proj(yv, M, (T)g.lbd);
+  T nrm = T(0);
+#pragma unroll
+  for (int j = 0; j < M; ++j) nrm += yv[j] * yv[j];
+  if (nrm > g.lbd2) {
+    const T sc = g.lbd / sqrt(nrm);
+#pragma unroll
+    for (int j = 0; j < M; ++j) yv[j] *= sc;
+  }
 }
 
 template <typename T>
-OPYX_D T tau_const(const Args<T>& a, const Geo& g) {
+OPYX_D T tau_const(const Args<T>& a, const Geo<T>& g) {
   return g.steps == OPYX_STEPS_ADAPTIVE ? (T)__ldg(&a.st->tau) : (T)a.tau;
 }
 template <typename T>
-OPYX_D T sigma_const(const Args<T>& a, const Geo& g) {
+OPYX_D T sigma_const(const Args<T>& a, const Geo<T>& g) {
   return g.steps == OPYX_STEPS_ADAPTIVE ? (T)__ldg(&a.st->sigma) : (T)a.sigma;
 }
 
@@ -164,13 +180,13 @@ OPYX_D T sigma_const(const Args<T>& a, const Geo& g) {
 // ADAPT = 1: reads xgrad (stored A^T y_k), x, f; writes x, xbar and
 //            gp = (x_k - x_{k+1})/tau - A^T y_k; reduces |gp|^2 into sums[1].
 template <typename T, int D, int C, int ADAPT>
-__global__ void __launch_bounds__(256) k_passA(Geo g, Args<T> a) {
+__global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
   double acc = 0.0;
   const T tau_c = tau_const(a, g);
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
-    coords<D>(g, r, q, c);
+    coords<T, D>(g, r, q, c);
     T div[C];
     if (ADAPT) {
 #pragma unroll
@@ -181,12 +197,12 @@ __global__ void __launch_bounds__(256) k_passA(Geo g, Args<T> a) {
     const bool on = !a.mask || a.mask[i];
 #pragma unroll
     for (int k = 0; k < C; ++k) {
-      const T tau = g.steps == OPYX_STEPS_PRECOND ? (T)precond_tau<D>(g, c, k) : tau_c;
+      const T tau = g.steps == OPYX_STEPS_PRECOND ? precond_tau<T, D>(g, c, k) : tau_c;
       const T xo = a.x[i * C + k];
       T xn = xo - tau * div[k];
-      if (on) xn = ssd_prox_value(xn, a.f[i * C + k], tau * (T)g.vol[k]);
+      if (on) xn = ssd_prox_value(xn, a.f[i * C + k], tau * g.vol[k]);
       a.x[i * C + k] = xn;
-      a.xbar[i * C + k] = (T)(1.0 + g.theta) * xn - (T)g.theta * xo;
+      a.xbar[i * C + k] = g.theta1 * xn - g.theta * xo;
       if (ADAPT) {
         const T gpk = (xo - xn) / tau - div[k];
         a.gp[i * C + k] = gpk;
@@ -210,21 +226,21 @@ __global__ void __launch_bounds__(256) k_passA(Geo g, Args<T> a) {
 //            |g_d|^2 = |(y_k - y_{k+1})/sigma - theta*A x_k + (theta+1)*A x_{k+1}|^2
 //            into sums[2], sums[3]  (pdhg.py:157-162).
 template <typename T, int D, int C, int ADAPT>
-__global__ void __launch_bounds__(256) k_passB(Geo g, Args<T> a) {
+__global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
   constexpr int M = D * C;
   double acc_r = 0.0, acc_g = 0.0;
   const T sig_c = sigma_const(a, g);
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
-    coords<D>(g, r, q, c);
+    coords<T, D>(g, r, q, c);
     T gb[M], yv[M], yo[M], sig[M];
     grad_at<T, D, C>(g, a.xbar, i, c, gb);
 #pragma unroll
     for (int t = 0; t < D; ++t) {
 #pragma unroll
       for (int k = 0; k < C; ++k) {
-        sig[t * C + k] = g.steps == OPYX_STEPS_PRECOND ? (T)precond_sigma<D>(g, c, t, k) : sig_c;
+        sig[t * C + k] = g.steps == OPYX_STEPS_PRECOND ? precond_sigma<T, D>(g, c, t, k) : sig_c;
       }
     }
 #pragma unroll
@@ -238,7 +254,7 @@ __global__ void __launch_bounds__(256) k_passB(Geo g, Args<T> a) {
     if (ADAPT) {
       T gn[M];
       grad_at<T, D, C>(g, a.x, i, c, gn);
-      const T th = (T)g.theta;
+      const T th = g.theta;
 #pragma unroll
       for (int j = 0; j < M; ++j) {
         // A x_k from xbar = (1+theta) x_{k+1} - theta x_k
@@ -266,12 +282,12 @@ __global__ void __launch_bounds__(256) k_passB(Geo g, Args<T> a) {
 // Adaptive only: xgrad = A^T y_{k+1}; RESID = 1 also reduces
 // |r_p|^2 = |gp + A^T y_{k+1}|^2 into sums[0] and applies the step rule.
 template <typename T, int D, int C, int RESID>
-__global__ void __launch_bounds__(256) k_passR(Geo g, Args<T> a) {
+__global__ void __launch_bounds__(256) k_passR(Geo<T> g, Args<T> a) {
   double acc = 0.0;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
-    coords<D>(g, r, q, c);
+    coords<T, D>(g, r, q, c);
     T div[C];
     div_at<T, D, C>(g, a.y, i, c, div);
 #pragma unroll
@@ -300,40 +316,45 @@ __global__ void __launch_bounds__(256) k_passR(Geo g, Args<T> a) {
 // the reference's conjugate SSD (functionals/quad.py:18-24) without the
 // cancellation of its two large sums.
 template <typename T, int D, int C>
-__global__ void __launch_bounds__(256) k_gap(Geo g, Args<T> a, double ssd_shift) {
+__global__ void __launch_bounds__(256) k_gap(Geo<T> g, Args<T> a, double ssd_shift) {
   constexpr int M = D * C;
   double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
-    coords<D>(g, r, q, c);
+    coords<T, D>(g, r, q, c);
     T ax[M], div[C];
     grad_at<T, D, C>(g, a.x, i, c, ax);
     div_at<T, D, C>(g, a.y, i, c, div);
     const bool on = !a.mask || a.mask[i];
     if (on) {
+      T pg = T(0), ps = T(0);
 #pragma unroll
       for (int k = 0; k < C; ++k) {
-        const double d = (double)a.x[i * C + k] - (double)a.f[i * C + k];
-        sG += 0.5 * g.vol[k] * d * d;
-        const double ak = (double)div[k];
-        sGs += ak * ak / (2.0 * g.vol[k]) - (double)a.f[i * C + k] * ak;
+        const T fk = a.f[i * C + k];
+        const T d = a.x[i * C + k] - fk;
+        pg += g.vol[k] * d * d;
+        ps += div[k] * div[k] * g.half_rvol[k] - fk * div[k];
       }
+      sG += 0.5 * (double)pg;
+      sGs += (double)ps;
     }
-    double n2 = 0.0, y2 = 0.0;
+    T n2 = T(0), y2 = T(0);
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-      n2 += (double)ax[j] * (double)ax[j];
-      const double yj = (double)a.y[i * M + j];
+      n2 += ax[j] * ax[j];
+      const T yj = a.y[i * M + j];
       y2 += yj * yj;
     }
-    const double nrm = sqrt(n2);
-    if (g.huber > 0)
-      sF += nrm <= g.huber ? 0.5 * n2 / g.huber : nrm - 0.5 * g.huber;
+    const T nrm = sqrt(n2);
+    T fv;
+    if (g.use_huber)
+      fv = nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber;
     else
-      sF += nrm;
-    sFs += y2;
-    inf = fmax(inf, sqrt(y2) - g.lbd);
+      fv = nrm;
+    sF += (double)fv;
+    sFs += (double)y2;
+    inf = fmax(inf, (double)(sqrt(y2) - g.lbd));
   }
   double vals[5] = {sG, sF, sGs, sFs, inf};
   const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
@@ -341,9 +362,9 @@ __global__ void __launch_bounds__(256) k_gap(Geo g, Args<T> a, double ssd_shift)
   const opyx_adaptive_state* st = a.st;
   block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
     const double Gx = tot[0] + ssd_shift;
-    const double FAx = g.lbd * tot[1];
+    const double FAx = g.lbd_d * tot[1];
     const double Gs = tot[2] - ssd_shift;
-    const double Fs = g.huber > 0 ? 0.5 * g.huber / g.lbd * tot[3] : 0.0;
+    const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
     info->objp = Gx + FAx;
     info->objd = -Gs - Fs;
     info->infeasp = 0.0;

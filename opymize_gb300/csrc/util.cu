@@ -41,6 +41,13 @@ __global__ void k_abs(int64_t n, const T* __restrict__ x, T* __restrict__ y) {
     y[i] = x[i] < T(0) ? -x[i] : x[i];
 }
 
+template <typename S, typename D>
+__global__ void k_cast(int64_t n, const S* __restrict__ x, D* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (D)x[i];
+}
+
 template <typename T>
 __global__ void k_recip_positive(int64_t n, T* __restrict__ x, double eps) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -126,6 +133,23 @@ int opyx_abs(int dtype, int64_t n, const void* x, void* y, void* stream) {
   if (n == 0) return OPYX_OK;
   OPYX_DISPATCH(dtype, T, (k_abs<T><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
                               n, (const T*)x, (T*)y)));
+  return check_launch();
+}
+
+int opyx_cast(int src_dtype, int dst_dtype, int64_t n, const void* x, void* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return OPYX_ERR_ARG;
+  if (n == 0) return OPYX_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned g = grid_for(n, 256);
+  if (src_dtype == OPYX_F64 && dst_dtype == OPYX_F32)
+    k_cast<double, float><<<g, 256, 0, s>>>(n, (const double*)x, (float*)y);
+  else if (src_dtype == OPYX_F32 && dst_dtype == OPYX_F64)
+    k_cast<float, double><<<g, 256, 0, s>>>(n, (const float*)x, (double*)y);
+  else if (src_dtype == dst_dtype && (src_dtype == OPYX_F32 || src_dtype == OPYX_F64))
+    return cudaMemcpyAsync(y, x, (size_t)n * (src_dtype == OPYX_F32 ? 4 : 8),
+                           cudaMemcpyDeviceToDevice, s) == cudaSuccess ? OPYX_OK : OPYX_ERR_LAUNCH;
+  else
+    return OPYX_ERR_ARG;
   return check_launch();
 }
 

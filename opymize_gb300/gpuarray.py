@@ -73,7 +73,18 @@ class DeviceArray(object):
 
     @classmethod
     def to_gpu(cls, ary, dtype=None):
-        ary = np.ascontiguousarray(ary, dtype=dtype)
+        ary = np.asarray(ary)
+        want = np.dtype(dtype) if dtype is not None else ary.dtype
+        floats = (np.dtype(np.float32), np.dtype(np.float64))
+        if ary.dtype != want and ary.dtype in floats and want in floats:
+            # upload in the host precision, convert on the device
+            src = cls.to_gpu(ary)
+            out = cls.empty(ary.shape, want)
+            if src.size:
+                _lib.call("opyx_cast", dtype_code(ary.dtype), dtype_code(want), src.size,
+                          src.ptr, out.ptr, stream_ptr())
+            return out
+        ary = np.ascontiguousarray(ary, dtype=want)
         src = ary.view(np.uint8) if ary.dtype == np.bool_ else ary
         t = torch().from_numpy(src).to("cuda", non_blocking=False)
         return cls(t, np.uint8 if ary.dtype == np.bool_ else ary.dtype)
@@ -113,7 +124,12 @@ class DeviceArray(object):
 
     # --- host transfers
     def get(self, ary=None):
-        h = self.t.detach().cpu().numpy()
+        """Copy to the host (through page-locked memory from torch's
+        caching host allocator); synchronises."""
+        t = torch()
+        h = t.empty(tuple(self.t.shape), dtype=self.t.dtype, pin_memory=True)
+        h.copy_(self.t)
+        h = h.numpy()
         if ary is None:
             return h
         ary[...] = h.reshape(ary.shape)

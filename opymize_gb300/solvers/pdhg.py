@@ -69,6 +69,7 @@ class PDHG(object):
         self.info = {}
         i['xk'] = self.g.x.new(dtype=dtype)
         i['yk'] = self.f.x.new(dtype=dtype)
+        self._zero_start = continue_at is None
         if continue_at is not None:
             i['xk'][:], i['yk'][:] = continue_at
         if term_maxiter == 0:
@@ -178,8 +179,7 @@ class PDHG(object):
         i = self.itervars
         A = self.linop
         N, C, D = int(np.prod(A.imagedims)), A.nchannels, len(A.imagedims)
-        x = DeviceArray.to_gpu(i['xk'], dtype)
-        y = DeviceArray.to_gpu(i['yk'], dtype)
+        x, y = self._start(dtype)
         xbar = DeviceArray.empty((N * C,), dtype)
         fdev = self.g.f_dev(dtype)
         mask = self.g.mask_dev()
@@ -253,6 +253,14 @@ class PDHG(object):
         self.info['time_s'] = el
         self.info['it_per_s'] = it / el if el > 0 else float('inf')
 
+    def _start(self, dtype):
+        """Device copies of the start point (zeros are filled on the device)."""
+        i = self.itervars
+        if self._zero_start:
+            return (DeviceArray.zeros((i['xk'].size,), dtype),
+                    DeviceArray.zeros((i['yk'].size,), dtype))
+        return DeviceArray.to_gpu(i['xk'], dtype), DeviceArray.to_gpu(i['yk'], dtype)
+
     def _download(self, x, y):
         self.itervars['xk'] = x.get().reshape(self.itervars['xk'].shape)
         self.itervars['yk'] = y.get().reshape(self.itervars['yk'].shape)
@@ -262,8 +270,7 @@ class PDHG(object):
                        term_maxiter, granularity, cbfun):
         i, c = self.itervars, self.constvars
         v = {}
-        v['xk'] = DeviceArray.to_gpu(i['xk'], dtype)
-        v['yk'] = DeviceArray.to_gpu(i['yk'], dtype)
+        v['xk'], v['yk'] = self._start(dtype)
         for s_ in ('xkp1', 'xgradk', 'xgradkp1'):
             v[s_] = DeviceArray.empty((self.g.x.size,), dtype)
         for s_ in ('ykp1', 'ygradk', 'ygradkp1'):

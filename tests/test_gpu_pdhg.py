@@ -75,7 +75,10 @@ def test_fp64_matches_reference(case, fused):
         for k in ("objp", "objd", "gap"):
             ref = d["info_" + k][j]
             assert abs(info[k] - ref) <= 1e-10 * max(1.0, abs(ref)), (case, k, it, info[k], ref)
-        if str(d["steps"]) == "adaptive":
+        # once the iterate has converged to roundoff, the adaptive rule
+        # branches on rounding noise, so the step sequence is compared only
+        # before that
+        if str(d["steps"]) == "adaptive" and abs(d["info_relgap"][j]) > 1e-10:
             assert abs(rec[int(it)][3] - d["info_tau"][j]) <= 1e-12 * d["info_tau"][j]
 
 
@@ -100,7 +103,8 @@ def test_fp32_adaptive_matches_reference(case):
     solver, rec = run_gpu(d, "float")
     for j, it in enumerate(d["dump_iters"]):
         x, y, info, tau = rec[int(it)]
-        assert abs(tau - d["info_tau"][j]) <= 1e-6 * d["info_tau"][j], (case, it)
+        if abs(d["info_relgap"][j]) > 1e-6:
+            assert abs(tau - d["info_tau"][j]) <= 1e-6 * d["info_tau"][j], (case, it)
         assert rel(x, d["x"][j]) <= 1e-5, (case, it, rel(x, d["x"][j]))
         assert rel(y, d["y"][j]) <= 1e-5, (case, it, rel(y, d["y"][j]))
 
@@ -112,12 +116,14 @@ def test_rof_gray256_adaptive_1000(precision, tol):
     d = np.load(os.path.join(GOLDEN, "rof_gray256_adaptive.npz"))
     solver, rec = run_gpu(d, precision)
     assert solver.path == "fused"
+    taus = np.array([rec[int(it)][3] for it in d["info_iters"]])
+    assert np.max(np.abs(taus - d["info_tau"]) / d["info_tau"]) <= \
+        (1e-12 if precision == "double" else 1e-6), (taus, d["info_tau"])
     x, y, info, tau = rec[1000]
     assert rel(x, d["x"][0]) <= tol, rel(x, d["x"][0])
     assert rel(y, d["y"][0]) <= tol, rel(y, d["y"][0])
     gaps = np.array([rec[int(it)][2]["relgap"] for it in d["info_iters"]])
-    assert np.max(np.abs(gaps - d["info_relgap"]) / np.abs(d["info_relgap"])) <= \
-        (1e-9 if precision == "double" else 1e-2)
+    assert np.max(np.abs(gaps - d["info_relgap"])) <= (1e-12 if precision == "double" else 1e-7)
 
 
 def test_graph_and_eager_agree():
@@ -150,4 +156,4 @@ def test_fused_matches_oracle_on_large_colour_problem():
     so.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=30, granularity=10)
     assert rel(s.state[0], so.state[0]) <= 1e-12
     assert rel(s.state[1], so.state[1]) <= 1e-12
-    assert abs(s.info["relgap"] - so.info["relgap"]) <= 1e-9 * abs(so.info["relgap"])
+    assert abs(s.info["relgap"] - so.info["relgap"]) <= 1e-10
