@@ -35,7 +35,9 @@ enum {
   OPYX_ERR_LAUNCH = 2,        /* CUDA launch / runtime error                  */
   OPYX_ERR_UNSUPPORTED = 3,   /* valid request this build does not implement */
   OPYX_ERR_WORKSPACE = 4,     /* workspace too small or misaligned           */
-  OPYX_ERR_NOT_CONVERGED = 5  /* an iterative device routine hit its bound   */
+  OPYX_ERR_NOT_CONVERGED = 5, /* an iterative device routine hit its bound   */
+  OPYX_ERR_SCRATCH_LIMIT = 6  /* problem exceeds the static scratch of
+                                 opyx_rof_iterate_noalloc                     */
 };
 
 enum { OPYX_F32 = 0, OPYX_F64 = 1 };
@@ -327,6 +329,26 @@ int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int i
  * adaptive residual pass R), for per-kernel timing and profiling. */
 int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   void* stream);
+/* Allocation-free variant of opyx_rof_init + opyx_rof_iterate (+ opyx_rof_gap).
+ * It has no counterpart in the reference: it serves callers that cannot
+ * allocate device memory (code running inside another framework's memory
+ * pool, or hosts that only receive device pointers for f, x and y).  The
+ * scratch -- step/info/reduction workspace, xbar and, for adaptive steps,
+ * A^T y and the residual part -- is a file-scope __device__ array of
+ * OPYX_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  Limit: the workspace (about 161 KiB) plus one
+ * (const / precond) or three (adaptive) N*C iterate arrays must fit, e.g.
+ * N*C <= 8,347,456 FP32 values for precond steps; larger problems return
+ * OPYX_ERR_SCRATCH_LIMIT before any launch.  Each call starts a fresh
+ * segment from the x, y it is given (step state from `p`), runs `iters`
+ * iterations and, if `gap_out` (device double[6]) is not NULL, writes
+ * objp, objd, infeasp, infeasd, gap, relgap there.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race. */
+#define OPYX_NOALLOC_SCRATCH_BYTES (32u << 20)
+int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void* y, const void* f,
+                             const uint8_t* mask, int iters, double* gap_out, void* stream);
 /* Primal-dual gap of the current iterate into the workspace's info record
  * (FP64 device reductions; pdhg.py:23-44, :287-305). */
 int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);

@@ -2,6 +2,8 @@
 // over (dtype, D, C) and the per-iteration launch sequence.
 #include <string.h>
 
+#include <mutex>
+
 #include "rof_kernels.cuh"
 
 namespace opyx {
@@ -278,3 +280,84 @@ int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* str
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers of this path cannot allocate device memory themselves: code
+// that runs inside another framework's memory pool or a host process that
+// is only handed device pointers for the image and the iterates.  For them
+// the scratch of the fused iteration -- the step/info/reduction workspace,
+// the extrapolated primal xbar and, for adaptive steps, A^T y and the
+// residual part -- lives in one file-scope __device__ array of
+// OPYX_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds
+// until the process exits.
+// ---------------------------------------------------------------------------
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[OPYX_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch for the current device, looked up once
+// per device with that device current (host code may not use the symbol's
+// name as an address).
+static int noalloc_scratch(char** out) {
+  static std::mutex mu;
+  static char* addr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OPYX_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr)
+      return OPYX_ERR_LAUNCH;
+    addr[dev] = (char*)ptr;
+  }
+  *out = addr[dev];
+  return OPYX_OK;
+}
+
+static size_t round256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+extern "C" int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void* y,
+                                        const void* f, const uint8_t* mask, int iters,
+                                        double* gap_out, void* stream) {
+  if (!p || iters < 0) return OPYX_ERR_ARG;
+  if (p->ndim < 1 || p->ndim > 3 || p->nchannels < 1 || p->nchannels > OPYX_ROF_MAX_C)
+    return OPYX_ERR_UNSUPPORTED;
+  int64_t N = 1;
+  for (int t = 0; t < p->ndim; ++t) {
+    if (p->dims[t] < 1) return OPYX_ERR_ARG;
+    N *= p->dims[t];
+  }
+  const size_t esz = p->dtype == OPYX_F64 ? 8 : 4;
+  const size_t field = round256((size_t)N * p->nchannels * esz);
+  const int nfields = p->steps == OPYX_STEPS_ADAPTIVE ? 3 : 1;   // xbar [, xgrad, gp]
+  if (N > (int64_t)(OPYX_NOALLOC_SCRATCH_BYTES / 4) ||
+      round256(kWsBytes) + nfields * field > (size_t)OPYX_NOALLOC_SCRATCH_BYTES)
+    return OPYX_ERR_SCRATCH_LIMIT;
+  char* base = nullptr;
+  int st = noalloc_scratch(&base);
+  if (st) return st;
+  opyx_rof_buffers b;
+  b.x = x;
+  b.y = y;
+  b.f = f;
+  b.mask = mask;
+  b.ws = base;
+  b.xbar = base + round256(kWsBytes);
+  b.xgrad = nfields > 1 ? base + round256(kWsBytes) + field : nullptr;
+  b.gp = nfields > 1 ? base + round256(kWsBytes) + 2 * field : nullptr;
+  // opyx_rof_init clears the info record and the reduction ticket, which the
+  // previous call left behind, and rewrites the step state.
+  st = opyx_rof_init(p, &b, stream);
+  if (st) return st;
+  st = opyx_rof_iterate(p, &b, iters, stream);
+  if (st) return st;
+  if (gap_out) {
+    st = opyx_rof_gap(p, &b, stream);
+    if (st) return st;
+    if (cudaMemcpyAsync(gap_out, base + kInfoOff, 6 * sizeof(double), cudaMemcpyDeviceToDevice,
+                        (cudaStream_t)stream) != cudaSuccess)
+      return OPYX_ERR_LAUNCH;
+  }
+  return OPYX_OK;
+}

@@ -105,6 +105,8 @@ const char* opyx_status_string(int s) {
     case OPYX_ERR_UNSUPPORTED: return "unsupported by this build";
     case OPYX_ERR_WORKSPACE: return "workspace too small or misaligned";
     case OPYX_ERR_NOT_CONVERGED: return "iterative device routine hit its iteration bound";
+    case OPYX_ERR_SCRATCH_LIMIT:
+      return "problem larger than the static scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }
