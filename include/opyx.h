@@ -295,6 +295,10 @@ typedef struct {
   double theta;                     /* overrelaxation (the reference uses 1) */
   double alpha0, eta, Delta;        /* adaptive rule (0.5, 0.95, 1.5)        */
   double eps[4];                    /* adaptive tolerances (pdhg.py:275-280) */
+  int32_t rows_per_thread;          /* tile height of the vectorised FP32
+                                       kernels; 0 = automatic               */
+  int32_t flags;                    /* bit 0: never use the vectorised FP32
+                                       kernels (for cross-checks)           */
 } opyx_rof_problem;
 
 typedef struct {

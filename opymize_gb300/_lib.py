@@ -72,7 +72,8 @@ class opyx_rof_problem(C.Structure):
                 ("ssd_shift", C.c_double), ("lbd", C.c_double), ("huber_alpha", C.c_double),
                 ("tau", C.c_double), ("sigma", C.c_double), ("theta", C.c_double),
                 ("alpha0", C.c_double), ("eta", C.c_double), ("Delta", C.c_double),
-                ("eps", C.c_double * 4)]
+                ("eps", C.c_double * 4), ("rows_per_thread", C.c_int32),
+                ("flags", C.c_int32)]
 
 
 class opyx_rof_buffers(C.Structure):

@@ -5,6 +5,7 @@
 #include <mutex>
 
 #include "rof_kernels.cuh"
+#include "rof_vec.cuh"
 
 namespace opyx {
 namespace rof {
@@ -128,6 +129,58 @@ static void shape(const Geo<T>& g, dim3* grid, dim3* block, bool reduce) {
   *grid = dim3((unsigned)gx, (unsigned)gy, 1);   // gx * gy <= cap_total
 }
 
+// The vectorised FP32 kernels need the contiguous axis to be a multiple of 4
+// and 16-byte aligned arrays (4-byte aligned mask).
+template <typename T>
+static bool vec_ok(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  if (p->dtype != OPYX_F32 || (p->flags & 1)) return false;
+  if (p->dims[p->ndim - 1] % 4 != 0) return false;
+  // the gap reduction has at most kMaxBlocks blocks and the vectorised
+  // kernels do not stride along the contiguous axis
+  if ((p->dims[p->ndim - 1] / 4 + kVecThreads - 1) / kVecThreads > kMaxBlocks) return false;
+  const uintptr_t al = (uintptr_t)b->x | (uintptr_t)b->xbar | (uintptr_t)b->y | (uintptr_t)b->f;
+  if (al & 15) return false;
+  if (b->mask && ((uintptr_t)b->mask & 3)) return false;
+  return true;
+}
+
+// Rows per thread of the vectorised kernels: enough warps to fill the GPU
+// (about 48 per SM), at most 16 rows; `p->rows_per_thread` > 0 overrides.
+template <typename T>
+static int rows_per_thread(const opyx_rof_problem* p, const Geo<T>& g) {
+  if (p->rows_per_thread > 0) return p->rows_per_thread;
+  const int64_t warps_per_row = ((g.nl >> 2) + 31) / 32;
+  const int64_t target = (int64_t)sm_count() * 48;
+  int64_t R = g.rows * warps_per_row / (target > 0 ? target : 1);
+  if (R < 1) R = 1;
+  if (R > 16) R = 16;
+  return (int)R;
+}
+
+template <typename T, int D, int C>
+struct VecLaunch {
+  static void run(const Geo<T>&, const Args<T>&, int, int, double, cudaStream_t) {}
+};
+
+template <int D, int C>
+struct VecLaunch<float, D, C> {
+  static void run(const Geo<float>& g, const Args<float>& a, int which, int R, double shift,
+                  cudaStream_t s) {
+    const int64_t Q = g.nl >> 2;
+    const int64_t gx = (Q + kVecThreads - 1) / kVecThreads;
+    int64_t gy = (g.rows + R - 1) / R;
+    const int64_t cap = which == 3 ? kMaxBlocks : (int64_t)sm_count() * 256;
+    int64_t cap_y = cap / gx;
+    if (cap_y < 1) cap_y = 1;
+    if (gy > cap_y) gy = cap_y;
+    if (gy > 65535) gy = 65535;
+    const dim3 grid((unsigned)gx, (unsigned)gy, 1), block(kVecThreads, 1, 1);
+    if (which == 0) k_passA_v<D, C><<<grid, block, 0, s>>>(g, a, R);
+    else if (which == 1) k_passB_v<D, C><<<grid, block, 0, s>>>(g, a, R);
+    else k_gap_v<D, C><<<grid, block, 0, s>>>(g, a, R, shift);
+  }
+};
+
 template <typename T, int D, int C>
 struct Runner {
   static int init(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
@@ -142,54 +195,57 @@ struct Runner {
     return OPYX_OK;
   }
 
+  // which: 0 = pass A, 1 = pass B, 2 = pass R (adaptive), 3 = gap
+  static void launch(const opyx_rof_problem* p, const Geo<T>& g, const Args<T>& a, int which,
+                     bool use_vec, int R, cudaStream_t s) {
+    const bool ad = p->steps == OPYX_STEPS_ADAPTIVE;
+    if (use_vec && (which == 3 || !ad)) {
+      VecLaunch<T, D, C>::run(g, a, which, R, p->ssd_shift, s);
+      return;
+    }
+    dim3 grid, block;
+    shape(g, &grid, &block, ad || which == 3);
+    if (which == 0) {
+      if (ad) k_passA<T, D, C, 1><<<grid, block, 0, s>>>(g, a);
+      else k_passA<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+    } else if (which == 1) {
+      if (ad) k_passB<T, D, C, 1><<<grid, block, 0, s>>>(g, a);
+      else k_passB<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
+    } else if (which == 2) {
+      k_passR<T, D, C, 1><<<grid, block, 0, s>>>(g, a);
+    } else {
+      k_gap<T, D, C><<<grid, block, 0, s>>>(g, a, p->ssd_shift);
+    }
+  }
+
   static int iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
                      cudaStream_t s) {
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    dim3 grid, block, rgrid, rblock;
-    shape(g, &grid, &block, false);
-    shape(g, &rgrid, &rblock, true);
+    const bool v = vec_ok<T>(p, b);
+    const int R = rows_per_thread(p, g);
     for (int it = 0; it < iters; ++it) {
-      if (p->steps == OPYX_STEPS_ADAPTIVE) {
-        k_passA<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-        k_passB<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-        k_passR<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-      } else {
-        k_passA<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
-        k_passB<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
-      }
+      launch(p, g, a, 0, v, R, s);
+      launch(p, g, a, 1, v, R, s);
+      if (p->steps == OPYX_STEPS_ADAPTIVE) launch(p, g, a, 2, v, R, s);
     }
     return check_launch();
   }
 
   static int pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   cudaStream_t s) {
+    if (which < 0 || which > 2 || (which == 2 && p->steps != OPYX_STEPS_ADAPTIVE))
+      return OPYX_ERR_ARG;
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    dim3 grid, block, rgrid, rblock;
-    shape(g, &grid, &block, false);
-    shape(g, &rgrid, &rblock, true);
-    const bool ad = p->steps == OPYX_STEPS_ADAPTIVE;
-    if (which == 0) {
-      if (ad) k_passA<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-      else k_passA<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
-    } else if (which == 1) {
-      if (ad) k_passB<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-      else k_passB<T, D, C, 0><<<grid, block, 0, s>>>(g, a);
-    } else if (which == 2 && ad) {
-      k_passR<T, D, C, 1><<<rgrid, rblock, 0, s>>>(g, a);
-    } else {
-      return OPYX_ERR_ARG;
-    }
+    launch(p, g, a, which, vec_ok<T>(p, b), rows_per_thread(p, g), s);
     return check_launch();
   }
 
   static int gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    dim3 grid, block;
-    shape(g, &grid, &block, true);
-    k_gap<T, D, C><<<grid, block, 0, s>>>(g, a, p->ssd_shift);
+    launch(p, g, a, 3, vec_ok<T>(p, b), rows_per_thread(p, g), s);
     return check_launch();
   }
 };

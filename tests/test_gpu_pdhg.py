@@ -179,6 +179,55 @@ def test_rof_gray256_fp32_replayed_steps():
     assert rel(y.get(), d["y"][0]) <= 1e-5, rel(y.get(), d["y"][0])
 
 
+@pytest.mark.parametrize("dims,C,huber,steps", [((512, 384), 3, 0.01, "precond"),
+                                                 ((200, 132), 1, 0.0, "const"),
+                                                 ((24, 36, 40), 1, 0.0, "precond"),
+                                                 ((4096,), 2, 0.02, "precond")])
+def test_vectorised_and_scalar_fp32_kernels_agree(dims, C, huber, steps):
+    """The 128-bit tiled FP32 passes and gap against the one-pixel-per-thread
+    kernels on the same problem (C-ABI flag bit 0 disables the tiles), and
+    both against the FP64 oracle."""
+    from opymize_gb300 import _lib
+    from opymize_gb300.gpuarray import DeviceArray, stream_ptr
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG
+    f = piecewise_constant(dims, C, sigma=0.1, seed=9)
+    N, D = int(np.prod(dims)), len(dims)
+    Fg = HuberL1Norms(N, (C, D), 0.07, huber) if huber > 0 else L1Norms(N, (C, D), 0.07)
+    s = PDHG(SSD(f.reshape(N, C)), Fg, GradientOp(dims, C, scheme="forward"))
+    s.constvars.update(theta=1.0, tau=0.3, sigma=0.4)
+    iters = 40
+    out = []
+    for flags in (0, 1):
+        p = s._rof_problem(np.float32, steps)
+        p.flags = flags
+        x = DeviceArray.zeros((N * C,), np.float32)
+        y = DeviceArray.zeros((N * D * C,), np.float32)
+        xbar = DeviceArray.zeros((N * C,), np.float32)
+        ws = DeviceArray.zeros(((_lib.load().opyx_rof_workspace_size() + 7) // 8,), np.float64)
+        fd = s.g.f_dev(np.float32)
+        b = _lib.opyx_rof_buffers()
+        b.x, b.xbar, b.y, b.f, b.ws = x.ptr, xbar.ptr, y.ptr, fd.ptr, ws.ptr
+        _lib.call("opyx_rof_init", p, b, stream_ptr())
+        _lib.call("opyx_rof_iterate", p, b, iters, stream_ptr())
+        _lib.call("opyx_rof_gap", p, b, stream_ptr())
+        off = _lib.load().opyx_rof_info_offset() // 8
+        out.append((x.get(), y.get(), ws[off:off + 6].get()))
+    (x0, y0, g0), (x1, y1, g1) = out
+    assert rel(x0, x1) <= 1e-6 and rel(y0, y1) <= 1e-6
+    assert abs(g0[5] - g1[5]) <= 1e-6 * max(1.0, abs(g1[5]))
+    Fo = oracle.HuberL1Norms(N, (C, D), 0.07, huber) if huber > 0 else oracle.L1Norms(N, (C, D), 0.07)
+    so = oracle.PDHG(oracle.SSD(f.reshape(N, C)), Fo, oracle.Gradient(dims, C, "forward"))
+    so.solve(steps=steps, term_pd_gap=1e-300, term_maxiter=iters, granularity=iters,
+             step_bound=0.12 if steps == "const" else None, step_factor=0.75)
+    if steps == "const":
+        return   # the oracle's const steps differ from the (tau, sigma) set above
+    assert rel(x0, so.state[0]) <= 1e-5 and rel(y0, so.state[1]) <= 1e-5
+    assert abs(g0[5] - so.info["relgap"]) <= 2e-6 + 1e-4 * abs(so.info["relgap"])
+
+
 def test_graph_and_eager_agree():
     d = np.load(os.path.join(GOLDEN, "c2d_huber_adaptive.npz"))
     _, r1 = run_gpu(d, "double", graph=True)
