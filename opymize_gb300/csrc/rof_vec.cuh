@@ -51,52 +51,6 @@ OPYX_D void zero(float (&d)[NF]) {
   for (int j = 0; j < NF; ++j) d[j] = 0.f;
 }
 
-// Warp-cooperative access to the warp's 32 consecutive quads of one row:
-// the chunk is contiguous (32 quads x E floats), so lane l moves float4
-// number j*32 + l -- every instruction covers 512 contiguous bytes -- and the
-// quads are handed out through shared memory.  `nvalid` = floats of the chunk
-// inside the row (partial last warp); the rest reads as 0 and is not stored.
-template <int E>
-OPYX_D void warp_load(float (&d)[E], const float* __restrict__ base, int64_t nvalid,
-                      float4* stage, int lane) {
-  static_assert(E % 4 == 0, "whole float4s");
-  const float4* gp = reinterpret_cast<const float4*>(base);
-#pragma unroll
-  for (int j = 0; j < E / 4; ++j) {
-    const int idx = j * 32 + lane;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if ((int64_t)idx * 4 < nvalid) v = gp[idx];
-    stage[idx] = v;
-  }
-  __syncwarp();
-#pragma unroll
-  for (int j = 0; j < E / 4; ++j) {
-    const float4 v = stage[lane * (E / 4) + j];
-    d[4 * j] = v.x;
-    d[4 * j + 1] = v.y;
-    d[4 * j + 2] = v.z;
-    d[4 * j + 3] = v.w;
-  }
-  __syncwarp();
-}
-
-template <int E>
-OPYX_D void warp_store(float* __restrict__ base, const float (&d)[E], int64_t nvalid,
-                       float4* stage, int lane) {
-  static_assert(E % 4 == 0, "whole float4s");
-#pragma unroll
-  for (int j = 0; j < E / 4; ++j)
-    stage[lane * (E / 4) + j] = make_float4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
-  __syncwarp();
-  float4* gp = reinterpret_cast<float4*>(base);
-#pragma unroll
-  for (int j = 0; j < E / 4; ++j) {
-    const int idx = j * 32 + lane;
-    if ((int64_t)idx * 4 < nvalid) gp[idx] = stage[idx];
-  }
-  __syncwarp();
-}
-
 // Row coordinates: crow along axis D-2, cz along axis 0 (D = 3).
 template <int D>
 OPYX_D void row_coords(const Geo<float>& g, int64_t r, int64_t* crow, int64_t* cz) {
@@ -105,72 +59,40 @@ OPYX_D void row_coords(const Geo<float>& g, int64_t r, int64_t* crow, int64_t* c
   if (D == 3) { *crow = r % g.n[1]; *cz = r / g.n[1]; }
 }
 
-// Per-warp view of the tile: the warp's first quad, its number of quads
-// inside the row and its shared staging buffer.
-template <int D, int C>
-struct WarpTile {
-  static constexpr int M = D * C;
-  float4* stage;
-  int lane;
-  int64_t qb;   // first quad of the warp
-  int64_t nq;   // quads of the warp inside the row (0..32)
-  OPYX_D int64_t nvx() const { return nq * 4 * C; }
-  OPYX_D int64_t nvy() const { return nq * 4 * M; }
-  // pixel index of the warp's first pixel in row r
-  OPYX_D int64_t base(const Geo<float>& g, int64_t r) const { return r * g.nl + qb * 4; }
-};
-
-template <int D, int C>
-OPYX_D WarpTile<D, C> warp_tile(const Geo<float>& g, float4* stage_all) {
-  WarpTile<D, C> w;
-  const int warp = threadIdx.x >> 5;
-  w.lane = threadIdx.x & 31;
-  w.stage = stage_all + warp * 32 * D * C;
-  w.qb = blockIdx.x * (int64_t)blockDim.x + warp * 32;
-  const int64_t Q = g.nl >> 2;
-  w.nq = Q - w.qb >= 32 ? 32 : (Q - w.qb > 0 ? Q - w.qb : 0);
-  return w;
-}
-
 // ------------------------------------------------------------------ pass B
 // y <- prox_{sigma F*}(y + sigma * A xbar) for R rows of one quad.
 template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<float> a, int R) {
   constexpr int M = D * C;
-  __shared__ float4 s_stage[(kVecThreads / 32) * 32 * M];
-  const WarpTile<D, C> w = warp_tile<D, C>(g, s_stage);
-  const int64_t quad = w.qb + w.lane;
-  const bool act = w.lane < w.nq;
+  const int64_t Q = g.nl >> 2;
+  const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool act = quad < Q;
   const int64_t q0 = quad * 4;
+  const int lane = threadIdx.x & 31;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const float sig_c = (float)a.sigma;
   for (int64_t r0 = blockIdx.y * (int64_t)R; r0 < g.rows; r0 += (int64_t)gridDim.y * R) {
     const int64_t rend = r0 + R < g.rows ? r0 + R : g.rows;
     float xc[4 * C];
-    warp_load<4 * C>(xc, a.xbar + w.base(g, r0) * C, w.nvx(), w.stage, w.lane);
+    if (act) ldv(xc, a.xbar + (r0 * g.nl + q0) * C); else zero(xc);
     for (int64_t r = r0; r < rend; ++r) {
-      const int64_t ib = w.base(g, r);
       const int64_t i0 = r * g.nl + q0;
       int64_t crow, cz;
       row_coords<D>(g, r, &crow, &cz);
       float xn[4 * C], xz[4 * C];
-      if (r + 1 < g.rows) warp_load<4 * C>(xn, a.xbar + (ib + g.nl) * C, w.nvx(), w.stage, w.lane);
-      else zero(xn);
+      if (act && r + 1 < g.rows) ldv(xn, a.xbar + (i0 + g.nl) * C); else zero(xn);
       const bool has_next = D >= 2 && crow < g.n[D - 2] - 1;
       const bool has_z = D == 3 && cz < g.n[0] - 1;
-      if (D == 3) {
-        if (has_z) warp_load<4 * C>(xz, a.xbar + (ib + g.s[0]) * C, w.nvx(), w.stage, w.lane);
-        else zero(xz);
-      }
+      if (D == 3) { if (act && has_z) ldv(xz, a.xbar + (i0 + g.s[0]) * C); else zero(xz); }
       float xr[C];
 #pragma unroll
       for (int k = 0; k < C; ++k) xr[k] = __shfl_down_sync(0xffffffffu, xc[k], 1);
-      if (w.lane == 31 && act && q0 + 4 < g.nl) {
+      if (lane == 31 && act && q0 + 4 < g.nl) {
 #pragma unroll
         for (int k = 0; k < C; ++k) xr[k] = a.xbar[(i0 + 4) * C + k];
       }
       float yv[4 * M];
-      warp_load<4 * M>(yv, a.y + ib * M, w.nvy(), w.stage, w.lane);
+      if (act) ldv(yv, a.y + i0 * M); else zero(yv);
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
         const bool inx = q0 + p < g.nl - 1;
@@ -206,7 +128,7 @@ __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<floa
           for (int j = 0; j < M; ++j) yv[p * M + j] *= sc;
         }
       }
-      warp_store<4 * M>(a.y + ib * M, yv, w.nvy(), w.stage, w.lane);
+      if (act) stv(a.y + i0 * M, yv);
 #pragma unroll
       for (int j = 0; j < 4 * C; ++j) xc[j] = xn[j];
     }
@@ -247,24 +169,22 @@ OPYX_D void quad_div(const Geo<float>& g, int64_t q0, int64_t crow, int64_t cz,
   }
 }
 
-// Backward neighbours needed by quad_div: the previous pixel's last-axis
-// component (warp shuffle; lane 0 loads it) and, for D = 3, the axis-0
-// component one plane back (a staged load of that plane's row).
+// Loads of the backward neighbours needed by quad_div.
 template <int D, int C>
-OPYX_D void quad_back(const Geo<float>& g, const float* __restrict__ y, const WarpTile<D, C>& w,
-                      bool act, int64_t ib, int64_t i0, int64_t q0, int64_t cz,
-                      const float (&yv)[4 * D * C], float (&yl)[C], float (&yz)[4 * C]) {
+OPYX_D void quad_back(const Geo<float>& g, const float* __restrict__ y, bool act, int lane,
+                      int64_t i0, int64_t q0, int64_t cz, const float (&yv)[4 * D * C],
+                      float (&yl)[C], float (&yz)[4 * C]) {
   constexpr int M = D * C;
 #pragma unroll
   for (int k = 0; k < C; ++k) yl[k] = __shfl_up_sync(0xffffffffu, yv[3 * M + (D - 1) * C + k], 1);
-  if (w.lane == 0 && act && q0 > 0) {
+  if (lane == 0 && act && q0 > 0) {
 #pragma unroll
     for (int k = 0; k < C; ++k) yl[k] = y[(i0 - 1) * M + (D - 1) * C + k];
   }
   if (D == 3) {
-    if (cz > 0) {
+    if (act && cz > 0) {
       float tmp[4 * M];
-      warp_load<4 * M>(tmp, y + (ib - g.s[0]) * M, w.nvy(), w.stage, w.lane);
+      ldv(tmp, y + (i0 - g.s[0]) * M);
 #pragma unroll
       for (int p = 0; p < 4; ++p)
 #pragma unroll
@@ -272,22 +192,6 @@ OPYX_D void quad_back(const Geo<float>& g, const float* __restrict__ y, const Wa
     } else {
       zero(yz);
     }
-  }
-}
-
-// Axis D-2 component of y in the row above r0 (start of a slide).
-template <int D, int C>
-OPYX_D void row_above(const Geo<float>& g, const float* __restrict__ y, const WarpTile<D, C>& w,
-                      int64_t r0, float (&yup)[4 * C]) {
-  constexpr int M = D * C;
-  zero(yup);
-  if (D >= 2 && r0 > 0) {
-    float tmp[4 * M];
-    warp_load<4 * M>(tmp, y + w.base(g, r0 - 1) * M, w.nvy(), w.stage, w.lane);
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-      for (int k = 0; k < C; ++k) yup[p * C + k] = tmp[p * M + (D - 2) * C + k];
   }
 }
 
@@ -304,47 +208,56 @@ OPYX_D float quad_tau(const Geo<float>& g, int64_t cl, int64_t crow, int64_t cz,
 template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_passA_v(Geo<float> g, Args<float> a, int R) {
   constexpr int M = D * C;
-  __shared__ float4 s_stage[(kVecThreads / 32) * 32 * M];
-  const WarpTile<D, C> w = warp_tile<D, C>(g, s_stage);
-  const int64_t quad = w.qb + w.lane;
-  const bool act = w.lane < w.nq;
+  const int64_t Q = g.nl >> 2;
+  const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool act = quad < Q;
   const int64_t q0 = quad * 4;
+  const int lane = threadIdx.x & 31;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const float tau_c = (float)a.tau;
   for (int64_t r0 = blockIdx.y * (int64_t)R; r0 < g.rows; r0 += (int64_t)gridDim.y * R) {
     const int64_t rend = r0 + R < g.rows ? r0 + R : g.rows;
     float yup[4 * C];
-    row_above<D, C>(g, a.y, w, r0, yup);
+    zero(yup);
+    if (D >= 2 && act && r0 > 0) {
+      float tmp[4 * M];
+      ldv(tmp, a.y + ((r0 - 1) * g.nl + q0) * M);
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int k = 0; k < C; ++k) yup[p * C + k] = tmp[p * M + (D - 2) * C + k];
+    }
     for (int64_t r = r0; r < rend; ++r) {
-      const int64_t ib = w.base(g, r);
       const int64_t i0 = r * g.nl + q0;
       int64_t crow, cz;
       row_coords<D>(g, r, &crow, &cz);
       float yv[4 * M];
-      warp_load<4 * M>(yv, a.y + ib * M, w.nvy(), w.stage, w.lane);
+      if (act) ldv(yv, a.y + i0 * M); else zero(yv);
       float yl[C], yz[4 * C];
-      quad_back<D, C>(g, a.y, w, act, ib, i0, q0, cz, yv, yl, yz);
+      quad_back<D, C>(g, a.y, act, lane, i0, q0, cz, yv, yl, yz);
       float dv[4 * C];
       quad_div<D, C>(g, q0, crow, cz, yv, yl, yup, yz, dv);
-      float xo[4 * C], fv[4 * C], xn[4 * C], xb[4 * C];
-      warp_load<4 * C>(xo, a.x + ib * C, w.nvx(), w.stage, w.lane);
-      warp_load<4 * C>(fv, a.f + ib * C, w.nvx(), w.stage, w.lane);
-      unsigned mk = 0xffffffffu;
-      if (a.mask && act) mk = *reinterpret_cast<const unsigned*>(a.mask + i0);
+      if (act) {
+        float xo[4 * C], fv[4 * C], xn[4 * C], xb[4 * C];
+        ldv(xo, a.x + i0 * C);
+        ldv(fv, a.f + i0 * C);
+        unsigned mk = 0xffffffffu;
+        if (a.mask) mk = *reinterpret_cast<const unsigned*>(a.mask + i0);
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        const bool on = (mk >> (8 * p)) & 0xffu;
+        for (int p = 0; p < 4; ++p) {
+          const bool on = (mk >> (8 * p)) & 0xffu;
 #pragma unroll
-        for (int k = 0; k < C; ++k) {
-          const float tau = pre ? quad_tau<D>(g, q0 + p, crow, cz, k) : tau_c;
-          float v = xo[p * C + k] - tau * dv[p * C + k];
-          if (on) v = ssd_prox_value(v, fv[p * C + k], tau * g.vol[k]);
-          xn[p * C + k] = v;
-          xb[p * C + k] = g.theta1 * v - g.theta * xo[p * C + k];
+          for (int k = 0; k < C; ++k) {
+            const float tau = pre ? quad_tau<D>(g, q0 + p, crow, cz, k) : tau_c;
+            float v = xo[p * C + k] - tau * dv[p * C + k];
+            if (on) v = ssd_prox_value(v, fv[p * C + k], tau * g.vol[k]);
+            xn[p * C + k] = v;
+            xb[p * C + k] = g.theta1 * v - g.theta * xo[p * C + k];
+          }
         }
+        stv(a.x + i0 * C, xn);
+        stv(a.xbar + i0 * C, xb);
       }
-      warp_store<4 * C>(a.x + ib * C, xn, w.nvx(), w.stage, w.lane);
-      warp_store<4 * C>(a.xbar + ib * C, xb, w.nvx(), w.stage, w.lane);
       if (D >= 2) {
 #pragma unroll
         for (int p = 0; p < 4; ++p)
@@ -362,51 +275,54 @@ template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_gap_v(Geo<float> g, Args<float> a, int R,
                                                        double ssd_shift) {
   constexpr int M = D * C;
-  __shared__ float4 s_stage[(kVecThreads / 32) * 32 * M];
-  const WarpTile<D, C> w = warp_tile<D, C>(g, s_stage);
-  const int64_t quad = w.qb + w.lane;
-  const bool act = w.lane < w.nq;
+  const int64_t Q = g.nl >> 2;
+  const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool act = quad < Q;
   const int64_t q0 = quad * 4;
+  const int lane = threadIdx.x & 31;
   double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
   for (int64_t r0 = blockIdx.y * (int64_t)R; r0 < g.rows; r0 += (int64_t)gridDim.y * R) {
     const int64_t rend = r0 + R < g.rows ? r0 + R : g.rows;
     float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;
     float yup[4 * C];
-    row_above<D, C>(g, a.y, w, r0, yup);
+    zero(yup);
+    if (D >= 2 && act && r0 > 0) {
+      float tmp[4 * M];
+      ldv(tmp, a.y + ((r0 - 1) * g.nl + q0) * M);
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int k = 0; k < C; ++k) yup[p * C + k] = tmp[p * M + (D - 2) * C + k];
+    }
     float xc[4 * C];
-    warp_load<4 * C>(xc, a.x + w.base(g, r0) * C, w.nvx(), w.stage, w.lane);
+    if (act) ldv(xc, a.x + (r0 * g.nl + q0) * C); else zero(xc);
     for (int64_t r = r0; r < rend; ++r) {
-      const int64_t ib = w.base(g, r);
       const int64_t i0 = r * g.nl + q0;
       int64_t crow, cz;
       row_coords<D>(g, r, &crow, &cz);
       // dual side: A^T y and y
       float yv[4 * M];
-      warp_load<4 * M>(yv, a.y + ib * M, w.nvy(), w.stage, w.lane);
+      if (act) ldv(yv, a.y + i0 * M); else zero(yv);
       float yl[C], yz[4 * C];
-      quad_back<D, C>(g, a.y, w, act, ib, i0, q0, cz, yv, yl, yz);
+      quad_back<D, C>(g, a.y, act, lane, i0, q0, cz, yv, yl, yz);
       float dv[4 * C];
       quad_div<D, C>(g, q0, crow, cz, yv, yl, yup, yz, dv);
       // primal side: A x
       float xn[4 * C], xz[4 * C];
-      if (r + 1 < g.rows) warp_load<4 * C>(xn, a.x + (ib + g.nl) * C, w.nvx(), w.stage, w.lane);
-      else zero(xn);
+      if (act && r + 1 < g.rows) ldv(xn, a.x + (i0 + g.nl) * C); else zero(xn);
       const bool has_next = D >= 2 && crow < g.n[D - 2] - 1;
       const bool has_z = D == 3 && cz < g.n[0] - 1;
-      if (D == 3) {
-        if (has_z) warp_load<4 * C>(xz, a.x + (ib + g.s[0]) * C, w.nvx(), w.stage, w.lane);
-        else zero(xz);
-      }
+      if (D == 3) { if (act && has_z) ldv(xz, a.x + (i0 + g.s[0]) * C); else zero(xz); }
       float xr[C];
 #pragma unroll
       for (int k = 0; k < C; ++k) xr[k] = __shfl_down_sync(0xffffffffu, xc[k], 1);
-      if (w.lane == 31 && act && q0 + 4 < g.nl) {
+      if (lane == 31 && act && q0 + 4 < g.nl) {
 #pragma unroll
         for (int k = 0; k < C; ++k) xr[k] = a.x[(i0 + 4) * C + k];
       }
-      float fv[4 * C];
-      warp_load<4 * C>(fv, a.f + ib * C, w.nvx(), w.stage, w.lane);
       if (act) {
+        float fv[4 * C];
+        ldv(fv, a.f + i0 * C);
         unsigned mk = 0xffffffffu;
         if (a.mask) mk = *reinterpret_cast<const unsigned*>(a.mask + i0);
 #pragma unroll
