@@ -298,7 +298,9 @@ typedef struct {
   int32_t rows_per_thread;          /* tile height of the vectorised FP32
                                        kernels; 0 = automatic               */
   int32_t flags;                    /* bit 0: never use the vectorised FP32
-                                       kernels (for cross-checks)           */
+                                       kernels; bit 1: never use the
+                                       row-streaming FP32 kernels (both for
+                                       cross-checks)                        */
 } opyx_rof_problem;
 
 typedef struct {

@@ -6,6 +6,7 @@
 
 #include "rof_kernels.cuh"
 #include "rof_vec.cuh"
+#include "rof_pipe.cuh"
 
 namespace opyx {
 namespace rof {
@@ -181,6 +182,59 @@ struct VecLaunch<float, D, C> {
   }
 };
 
+// Row-streaming kernels (rof_pipe.cuh): 2-D and 3-D FP32 problems whose
+// arrays satisfy the vector requirements; flag bit 1 turns them off.
+template <typename T>
+static bool pipe_ok(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  return p->ndim >= 2 && !(p->flags & 2) && vec_ok<T>(p, b);
+}
+
+template <typename T, int D, int C>
+struct PipeLaunch {
+  static void run(const Geo<T>&, const Args<T>&, int, double, cudaStream_t) {}
+};
+
+template <typename K>
+static int pipe_blocks_per_sm(K kernel, int smem) {
+  int n = 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kPipeThreads, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <int D, int C>
+struct PipeLaunch<float, D, C> {
+  // Grid: ceil(nl / TW) tiles across x; enough row runs for one full wave
+  // of resident CTAs.
+  template <typename K>
+  static void go(K kernel, int smem, const Geo<float>& g, const Args<float>& a, bool reduce,
+                 double shift, cudaStream_t s, int which) {
+    static int per_sm[3] = {-1, -1, -1};
+    if (per_sm[which] < 0) per_sm[which] = pipe_blocks_per_sm(kernel, smem);
+    const int64_t gx = (g.nl + kPipeTW - 1) / kPipeTW;
+    int64_t target = (int64_t)(per_sm[which] > 0 ? per_sm[which] : 1) * sm_count();
+    if (reduce && target > kMaxBlocks) target = kMaxBlocks;
+    int64_t gy = target / gx;
+    if (gy < 1) gy = 1;
+    if (gy > g.rows) gy = g.rows;
+    const int RB = (int)((g.rows + gy - 1) / gy);
+    gy = (g.rows + RB - 1) / RB;
+    const dim3 grid((unsigned)gx, (unsigned)gy, 1);
+    if (which == 0) k_passA_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB);
+    else if (which == 1) k_passB_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB);
+    else k_gap_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB, shift);
+  }
+  static void run(const Geo<float>& g, const Args<float>& a, int which, double shift,
+                  cudaStream_t s) {
+    using S = PipeSmem<D, C>;
+    if (which == 0) go(k_passA_p<D, C>, S::A, g, a, false, shift, s, 0);
+    else if (which == 1) go(k_passB_p<D, C>, S::B, g, a, false, shift, s, 1);
+    else go(k_gap_p<D, C>, S::G, g, a, true, shift, s, 2);
+  }
+};
+
 template <typename T, int D, int C>
 struct Runner {
   static int init(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
@@ -197,8 +251,12 @@ struct Runner {
 
   // which: 0 = pass A, 1 = pass B, 2 = pass R (adaptive), 3 = gap
   static void launch(const opyx_rof_problem* p, const Geo<T>& g, const Args<T>& a, int which,
-                     bool use_vec, int R, cudaStream_t s) {
+                     bool use_vec, int R, cudaStream_t s, bool use_pipe = false) {
     const bool ad = p->steps == OPYX_STEPS_ADAPTIVE;
+    if (use_pipe && (which == 3 || !ad) && D >= 2) {
+      PipeLaunch<T, D, C>::run(g, a, which == 3 ? 2 : which, p->ssd_shift, s);
+      return;
+    }
     if (use_vec && (which == 3 || !ad)) {
       VecLaunch<T, D, C>::run(g, a, which, R, p->ssd_shift, s);
       return;
@@ -222,12 +280,12 @@ struct Runner {
                      cudaStream_t s) {
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    const bool v = vec_ok<T>(p, b);
+    const bool v = vec_ok<T>(p, b), pp = pipe_ok<T>(p, b);
     const int R = rows_per_thread(p, g);
     for (int it = 0; it < iters; ++it) {
-      launch(p, g, a, 0, v, R, s);
-      launch(p, g, a, 1, v, R, s);
-      if (p->steps == OPYX_STEPS_ADAPTIVE) launch(p, g, a, 2, v, R, s);
+      launch(p, g, a, 0, v, R, s, pp);
+      launch(p, g, a, 1, v, R, s, pp);
+      if (p->steps == OPYX_STEPS_ADAPTIVE) launch(p, g, a, 2, v, R, s, pp);
     }
     return check_launch();
   }
@@ -238,14 +296,14 @@ struct Runner {
       return OPYX_ERR_ARG;
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    launch(p, g, a, which, vec_ok<T>(p, b), rows_per_thread(p, g), s);
+    launch(p, g, a, which, vec_ok<T>(p, b), rows_per_thread(p, g), s, pipe_ok<T>(p, b));
     return check_launch();
   }
 
   static int gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
-    launch(p, g, a, 3, vec_ok<T>(p, b), rows_per_thread(p, g), s);
+    launch(p, g, a, 3, vec_ok<T>(p, b), rows_per_thread(p, g), s, pipe_ok<T>(p, b));
     return check_launch();
   }
 };

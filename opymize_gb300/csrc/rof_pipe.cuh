@@ -1,0 +1,422 @@
+// Row-streaming FP32 kernels of the fused ROF passes and gap, with the
+// global->shared traffic in asynchronous copies (cp.async, 16 bytes per
+// instruction, zero-fill outside the image).
+//
+// A CTA owns a tile of TW pixels along the contiguous last axis and a run
+// of RB consecutive rows (row = all pixels with equal coordinates in the
+// other axes).  Each array it reads streams through a small ring of row
+// slots in shared memory: while the CTA computes row r, the copies of the
+// rows it needs next are already in flight, so memory stays busy without
+// holding data in registers.  Results go back to shared memory and leave in
+// coalesced 128-bit stores (each warp instruction covers 512 contiguous
+// bytes).  Neighbours along the last axis are read from the slot (slots carry
+// a 4-pixel halo), neighbours along axis D-2 are the adjacent row slots, and
+// for D = 3 the rows one plane away stream through rings of their own.
+//
+// All waits are cp.async.wait_group (hardware completion of this thread's
+// own copies); there is no spin loop.  Requirements (checked on the host):
+// last axis a multiple of 4, 16-byte aligned arrays, 4-byte aligned mask.
+#pragma once
+
+#include "rof_kernels.cuh"
+
+namespace opyx {
+namespace rof {
+
+constexpr int kPipeTW = 512;               // tile width in pixels
+constexpr int kPipeThreads = kPipeTW / 4;  // 4 pixels per thread
+
+OPYX_D void cp_async16(void* sdst, const void* gsrc, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  const int n = valid ? 16 : 0;   // 0: zero-fill, the source is not read
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gsrc), "r"(n)
+               : "memory");
+}
+OPYX_D void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+OPYX_D void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Cooperative copy of row `r` of an array with E floats per pixel into a slot
+// holding pixels [q_beg - HL, q_beg + TW + HR).  Chunks outside the row or
+// outside [0, rows) are zero-filled; `need` = false (a row past the end of
+// the CTA's run) issues nothing.
+template <int E, int HL, int HR>
+OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float>& g, int64_t r,
+                     int64_t q_beg, bool need = true) {
+  if (!need) return;
+  constexpr int NPX = kPipeTW + HL + HR;
+  constexpr int NCH = NPX * E / 4;
+  const bool rv = r >= 0 && r < g.rows;
+  const int64_t row_f0 = (rv ? r : 0) * g.nl * E;        // float offset of the row
+  const int64_t f0 = (q_beg - HL) * E;                    // float offset of the slot in the row
+  const int64_t fmax = g.nl * E;
+  for (int c = threadIdx.x; c < NCH; c += kPipeThreads) {
+    const int64_t fo = f0 + (int64_t)c * 4;
+    const bool valid = rv && fo >= 0 && fo + 4 <= fmax;
+    cp_async16(slot + c * 4, arr + row_f0 + (valid ? fo : 0), valid);
+  }
+}
+
+// Cooperative coalesced store of the first TW pixels (after HL halo pixels)
+// of a slot to row r.
+template <int E, int HL>
+OPYX_D void store_row(float* __restrict__ arr, const float* slot, const Geo<float>& g, int64_t r,
+                      int64_t q_beg) {
+  constexpr int NCH = kPipeTW * E / 4;
+  const int64_t f0 = q_beg * E;
+  const int64_t fmax = g.nl * E;
+  float* row = arr + r * g.nl * E;
+  const float4* s = reinterpret_cast<const float4*>(slot + HL * E);
+  for (int c = threadIdx.x; c < NCH; c += kPipeThreads) {
+    const int64_t fo = f0 + (int64_t)c * 4;
+    if (fo + 4 <= fmax) *reinterpret_cast<float4*>(row + fo) = s[c];
+  }
+}
+
+template <int D>
+OPYX_D void pipe_row_coords(const Geo<float>& g, int64_t r, int64_t* crow, int64_t* cz) {
+  if (D == 2) { *crow = r; *cz = 0; }
+  if (D == 3) { *crow = r % g.n[1]; *cz = r / g.n[1]; }
+}
+
+// Shared-memory sizes (bytes) of the three kernels.
+template <int D, int C>
+struct PipeSmem {
+  static constexpr int M = D * C;
+  static constexpr int X4 = (kPipeTW + 4) * C;   // floats of a slot with a 4-pixel halo
+  static constexpr int Y4 = (kPipeTW + 4) * M;
+  static constexpr int X0 = kPipeTW * C;
+  static constexpr int Y0 = kPipeTW * M;
+  // pass B: xbar ring 3 (halo right), y ring 2, [xbar plane ring 2]
+  static constexpr int B = 4 * (3 * X4 + 2 * Y0 + (D == 3 ? 2 * X0 : 0));
+  // pass A: y ring 3 (halo left), x ring 2, f ring 2, xbar out, [y plane ring 2]
+  static constexpr int A = 4 * (3 * Y4 + 2 * X0 + 2 * X0 + X0 + (D == 3 ? 2 * Y0 : 0));
+  // gap: x ring 3 (halo right), y ring 3 (halo left), f ring 2, [x, y plane rings]
+  static constexpr int G = 4 * (3 * X4 + 3 * Y4 + 2 * X0 + (D == 3 ? 2 * X0 + 2 * Y0 : 0));
+};
+
+// ------------------------------------------------------------------ pass B
+template <int D, int C>
+__global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<float> a, int RB) {
+  using S = PipeSmem<D, C>;
+  constexpr int M = D * C;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  float* xs = sm;                          // 3 x X4
+  float* ys = xs + 3 * S::X4;              // 2 x Y0
+  float* zs = ys + 2 * S::Y0;              // 2 x X0 (D = 3)
+  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int lp0 = threadIdx.x * 4;         // first local pixel of this thread
+  const bool pre = g.steps == OPYX_STEPS_PRECOND;
+  const float sig_c = (float)a.sigma;
+  const int64_t nplane = D == 3 ? g.n[1] : 0;  // rows per plane
+  for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
+    const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
+    copy_row<C, 0, 4>(xs, a.xbar, g, r0, q_beg);
+    copy_row<C, 0, 4>(xs + S::X4, a.xbar, g, r0 + 1, q_beg);
+    copy_row<M, 0, 0>(ys, a.y, g, r0, q_beg);
+    if (D == 3) copy_row<C, 0, 0>(zs, a.xbar, g, r0 + nplane, q_beg);
+    cp_commit();
+    for (int64_t r = r0; r < r1; ++r) {
+      const int k = (int)(r - r0);
+      // prefetch the rows of the next step
+      copy_row<C, 0, 4>(xs + ((k + 2) % 3) * S::X4, a.xbar, g, r + 2, q_beg, r + 2 <= r1);
+      copy_row<M, 0, 0>(ys + ((k + 1) & 1) * S::Y0, a.y, g, r + 1, q_beg, r + 1 < r1);
+      if (D == 3)
+        copy_row<C, 0, 0>(zs + ((k + 1) & 1) * S::X0, a.xbar, g, r + 1 + nplane, q_beg, r + 1 < r1);
+      cp_commit();
+      cp_wait<1>();
+      __syncthreads();
+      const float* xc = xs + (k % 3) * S::X4;
+      const float* xn = xs + ((k + 1) % 3) * S::X4;
+      float* yv = ys + (k & 1) * S::Y0;
+      const float* xz = zs + (k & 1) * S::X0;
+      int64_t crow, cz;
+      pipe_row_coords<D>(g, r, &crow, &cz);
+      const bool has_next = crow < g.n[D - 2] - 1;
+      const bool has_z = D == 3 && cz < g.n[0] - 1;
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int lp = lp0 + p;
+        const int64_t q = q_beg + lp;
+        const bool inx = q < g.nl - 1;
+        float yy[M], sg[M];
+#pragma unroll
+        for (int j = 0; j < M; ++j) yy[j] = yv[lp * M + j];
+#pragma unroll
+        for (int k2 = 0; k2 < C; ++k2) {
+          const float xk = xc[lp * C + k2];
+          const float gl = inx ? g.coef[D - 1][k2] * (xc[(lp + 1) * C + k2] - xk) : 0.f;
+          sg[(D - 1) * C + k2] = pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c;
+          yy[(D - 1) * C + k2] += sg[(D - 1) * C + k2] * gl;
+          const float gr = has_next ? g.coef[D - 2][k2] * (xn[lp * C + k2] - xk) : 0.f;
+          sg[(D - 2) * C + k2] = pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c;
+          yy[(D - 2) * C + k2] += sg[(D - 2) * C + k2] * gr;
+          if (D == 3) {
+            const float gz = has_z ? g.coef[0][k2] * (xz[lp * C + k2] - xk) : 0.f;
+            sg[k2] = pre ? (has_z ? g.sig_pre[0][k2] : 0.f) : sig_c;
+            yy[k2] += sg[k2] * gz;
+          }
+        }
+        if (g.use_huber) {
+#pragma unroll
+          for (int j = 0; j < M; ++j) yy[j] /= 1.f + sg[j] * g.hub_ratio;
+        }
+        float n2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < M; ++j) n2 += yy[j] * yy[j];
+        if (n2 > g.lbd2) {
+          const float sc = g.lbd / sqrtf(n2);
+#pragma unroll
+          for (int j = 0; j < M; ++j) yy[j] *= sc;
+        }
+#pragma unroll
+        for (int j = 0; j < M; ++j) yv[lp * M + j] = yy[j];
+      }
+      __syncthreads();
+      store_row<M, 0>(a.y, yv, g, r, q_beg);
+      __syncthreads();
+    }
+    cp_wait<0>();
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ pass A
+template <int D, int C>
+__global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<float> a, int RB) {
+  using S = PipeSmem<D, C>;
+  constexpr int M = D * C;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  float* ys = sm;                          // 3 x Y4 (halo left: local pixel = lp + 4)
+  float* xs = ys + 3 * S::Y4;              // 2 x X0
+  float* fs = xs + 2 * S::X0;              // 2 x X0
+  float* bs = fs + 2 * S::X0;              // 1 x X0 (xbar out)
+  float* zs = bs + S::X0;                  // 2 x Y0 (D = 3: y one plane back)
+  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int lp0 = threadIdx.x * 4;
+  const bool pre = g.steps == OPYX_STEPS_PRECOND;
+  const float tau_c = (float)a.tau;
+  const int64_t nplane = D == 3 ? g.n[1] : 0;
+  for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
+    const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
+    // y slot of row r is ((r - r0 + 1) % 3): row r0 - 1 -> 0, r0 -> 1, r0 + 1 -> 2
+    copy_row<M, 4, 0>(ys, a.y, g, r0 - 1, q_beg);
+    copy_row<M, 4, 0>(ys + S::Y4, a.y, g, r0, q_beg);
+    copy_row<C, 0, 0>(xs, a.x, g, r0, q_beg);
+    copy_row<C, 0, 0>(fs, a.f, g, r0, q_beg);
+    if (D == 3) copy_row<M, 0, 0>(zs, a.y, g, r0 - nplane, q_beg);
+    cp_commit();
+    for (int64_t r = r0; r < r1; ++r) {
+      const int k = (int)(r - r0);
+      const bool more = r + 1 < r1;
+      copy_row<M, 4, 0>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0>(xs + ((k + 1) & 1) * S::X0, a.x, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
+      if (D == 3) copy_row<M, 0, 0>(zs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
+      cp_commit();
+      cp_wait<1>();
+      __syncthreads();
+      const float* yc = ys + ((k + 1) % 3) * S::Y4;     // row r
+      const float* yu = ys + (k % 3) * S::Y4;           // row r - 1
+      float* xv = xs + (k & 1) * S::X0;
+      const float* fv = fs + (k & 1) * S::X0;
+      const float* yz = zs + (k & 1) * S::Y0;
+      int64_t crow, cz;
+      pipe_row_coords<D>(g, r, &crow, &cz);
+      const bool has_up = crow > 0, has_dn = crow < g.n[D - 2] - 1;
+      const bool has_zb = D == 3 && cz > 0, has_zf = D == 3 && cz < g.n[0] - 1;
+      unsigned mk = 0xffffffffu;
+      const int64_t qt = q_beg + lp0;
+      if (a.mask && qt < g.nl) mk = *reinterpret_cast<const unsigned*>(a.mask + r * g.nl + qt);
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int lp = lp0 + p;
+        const int ly = lp + 4;                      // index in the halo slots
+        const int64_t q = q_beg + lp;
+        const bool on = (mk >> (8 * p)) & 0xffu;
+#pragma unroll
+        for (int k2 = 0; k2 < C; ++k2) {
+          float s = 0.f;
+          const float ihl = g.invh[D - 1];
+          if (q < g.nl - 1) s -= yc[ly * M + (D - 1) * C + k2] * ihl;
+          if (q > 0) s += yc[(ly - 1) * M + (D - 1) * C + k2] * ihl;
+          const float ihr = g.invh[D - 2];
+          if (has_dn) s -= yc[ly * M + (D - 2) * C + k2] * ihr;
+          if (has_up) s += yu[ly * M + (D - 2) * C + k2] * ihr;
+          if (D == 3) {
+            const float ihz = g.invh[0];
+            if (has_zf) s -= yc[ly * M + k2] * ihz;
+            if (has_zb) s += yz[lp * M + k2] * ihz;
+          }
+          const float dv = g.w[k2] * s;
+          float tau = tau_c;
+          if (pre) {
+            float cs = g.absc[D - 1][k2] * (float)((q < g.nl - 1) + (q > 0)) +
+                       g.absc[D - 2][k2] * (float)(has_dn + has_up);
+            if (D == 3) cs += g.absc[0][k2] * (float)(has_zf + has_zb);
+            tau = cs > 2.220446049250313e-16f ? 1.f / cs : 0.f;
+          }
+          const float xo = xv[lp * C + k2];
+          float v = xo - tau * dv;
+          if (on) v = ssd_prox_value(v, fv[lp * C + k2], tau * g.vol[k2]);
+          xv[lp * C + k2] = v;
+          bs[lp * C + k2] = g.theta1 * v - g.theta * xo;
+        }
+      }
+      __syncthreads();
+      store_row<C, 0>(a.x, xv, g, r, q_beg);
+      store_row<C, 0>(a.xbar, bs, g, r, q_beg);
+      __syncthreads();
+    }
+    cp_wait<0>();
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ gap
+// The sums of k_gap; FP32 partials per thread over its pixels and rows,
+// FP64 across threads and blocks.
+template <int D, int C>
+__global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float> a, int RB,
+                                                        double ssd_shift) {
+  using S = PipeSmem<D, C>;
+  constexpr int M = D * C;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  float* xs = sm;                          // 3 x X4 (halo right)
+  float* ys = xs + 3 * S::X4;              // 3 x Y4 (halo left)
+  float* fs = ys + 3 * S::Y4;              // 2 x X0
+  float* xzs = fs + 2 * S::X0;             // 2 x X0 (D = 3: x one plane forward)
+  float* yzs = xzs + 2 * S::X0;            // 2 x Y0 (D = 3: y one plane back)
+  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int lp0 = threadIdx.x * 4;
+  const int64_t nplane = D == 3 ? g.n[1] : 0;
+  double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
+  for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
+    const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
+    float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;
+    // x slot of row r: (r - r0) % 3; y slot of row r: (r - r0 + 1) % 3
+    copy_row<C, 0, 4>(xs, a.x, g, r0, q_beg);
+    copy_row<C, 0, 4>(xs + S::X4, a.x, g, r0 + 1, q_beg);
+    copy_row<M, 4, 0>(ys, a.y, g, r0 - 1, q_beg);
+    copy_row<M, 4, 0>(ys + S::Y4, a.y, g, r0, q_beg);
+    copy_row<C, 0, 0>(fs, a.f, g, r0, q_beg);
+    if (D == 3) {
+      copy_row<C, 0, 0>(xzs, a.x, g, r0 + nplane, q_beg);
+      copy_row<M, 0, 0>(yzs, a.y, g, r0 - nplane, q_beg);
+    }
+    cp_commit();
+    for (int64_t r = r0; r < r1; ++r) {
+      const int k = (int)(r - r0);
+      const bool more = r + 1 < r1;
+      copy_row<C, 0, 4>(xs + ((k + 2) % 3) * S::X4, a.x, g, r + 2, q_beg, r + 2 <= r1);
+      copy_row<M, 4, 0>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
+      if (D == 3) {
+        copy_row<C, 0, 0>(xzs + ((k + 1) & 1) * S::X0, a.x, g, r + 1 + nplane, q_beg, more);
+        copy_row<M, 0, 0>(yzs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
+      }
+      cp_commit();
+      cp_wait<1>();
+      __syncthreads();
+      const float* xc = xs + (k % 3) * S::X4;
+      const float* xn = xs + ((k + 1) % 3) * S::X4;
+      const float* yc = ys + ((k + 1) % 3) * S::Y4;
+      const float* yu = ys + (k % 3) * S::Y4;
+      const float* fv = fs + (k & 1) * S::X0;
+      const float* xz = xzs + (k & 1) * S::X0;
+      const float* yz = yzs + (k & 1) * S::Y0;
+      int64_t crow, cz;
+      pipe_row_coords<D>(g, r, &crow, &cz);
+      const bool has_up = crow > 0, has_dn = crow < g.n[D - 2] - 1;
+      const bool has_zb = D == 3 && cz > 0, has_zf = D == 3 && cz < g.n[0] - 1;
+      unsigned mk = 0xffffffffu;
+      const int64_t qt = q_beg + lp0;
+      if (a.mask && qt < g.nl) mk = *reinterpret_cast<const unsigned*>(a.mask + r * g.nl + qt);
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int lp = lp0 + p, ly = lp + 4;
+        const int64_t q = q_beg + lp;
+        if (q >= g.nl) continue;
+        const bool on = (mk >> (8 * p)) & 0xffu;
+        const bool inx = q < g.nl - 1;
+        float n2 = 0.f, y2 = 0.f;
+#pragma unroll
+        for (int k2 = 0; k2 < C; ++k2) {
+          const float xk = xc[lp * C + k2], fk = fv[lp * C + k2];
+          // A^T y
+          float s = 0.f;
+          const float ihl = g.invh[D - 1], ihr = g.invh[D - 2];
+          if (inx) s -= yc[ly * M + (D - 1) * C + k2] * ihl;
+          if (q > 0) s += yc[(ly - 1) * M + (D - 1) * C + k2] * ihl;
+          if (has_dn) s -= yc[ly * M + (D - 2) * C + k2] * ihr;
+          if (has_up) s += yu[ly * M + (D - 2) * C + k2] * ihr;
+          if (D == 3) {
+            const float ihz = g.invh[0];
+            if (has_zf) s -= yc[ly * M + k2] * ihz;
+            if (has_zb) s += yz[lp * M + k2] * ihz;
+          }
+          const float ak = g.w[k2] * s;
+          if (on) {
+            const float d = xk - fk;
+            pG += g.vol[k2] * d * d;
+            pGs += ak * ak * g.half_rvol[k2] - fk * ak;
+          }
+          // A x
+          const float gl = inx ? g.coef[D - 1][k2] * (xc[(lp + 1) * C + k2] - xk) : 0.f;
+          const float gr = has_dn ? g.coef[D - 2][k2] * (xn[lp * C + k2] - xk) : 0.f;
+          n2 += gl * gl + gr * gr;
+          if (D == 3) {
+            const float gz = has_zf ? g.coef[0][k2] * (xz[lp * C + k2] - xk) : 0.f;
+            n2 += gz * gz;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+          const float yj = yc[ly * M + j];
+          y2 += yj * yj;
+        }
+        const float nrm = sqrtf(n2);
+        pF += g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
+        pFs += y2;
+        pinf = fmaxf(pinf, sqrtf(y2) - g.lbd);
+      }
+      __syncthreads();
+    }
+    cp_wait<0>();
+    __syncthreads();
+    sG += 0.5 * (double)pG;
+    sF += (double)pF;
+    sGs += (double)pGs;
+    sFs += (double)pFs;
+    inf = fmax(inf, (double)pinf);
+  }
+  double vals[5] = {sG, sF, sGs, sFs, inf};
+  const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
+  opyx_rof_info* info = a.info;
+  const opyx_adaptive_state* st = a.st;
+  block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
+    const double Gx = tot[0] + ssd_shift;
+    const double FAx = g.lbd_d * tot[1];
+    const double Gs = tot[2] - ssd_shift;
+    const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
+    info->objp = Gx + FAx;
+    info->objd = -Gs - Fs;
+    info->infeasp = 0.0;
+    info->infeasd = fmax(0.0, tot[4]);
+    info->gap = info->objp - info->objd;
+    info->relgap = info->gap / fmax(2.220446049250313e-16, fabs(info->objd));
+    info->tau = st->tau;
+    info->sigma = st->sigma;
+    info->alpha = st->alpha;
+    info->resp = st->resp;
+    info->resd = st->resd;
+    info->epsp = st->epsp;
+    info->epsd = st->epsd;
+  });
+}
+
+}  // namespace rof
+}  // namespace opyx

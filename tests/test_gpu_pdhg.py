@@ -200,7 +200,9 @@ def test_vectorised_and_scalar_fp32_kernels_agree(dims, C, huber, steps):
     s.constvars.update(theta=1.0, tau=0.3, sigma=0.4)
     iters = 40
     out = []
-    for flags in (0, 1):
+    # flags 0: row-streaming kernels (2-D/3-D) or quad kernels (1-D);
+    # 2: quad kernels; 1: one-pixel-per-thread kernels
+    for flags in (0, 1, 2):
         p = s._rof_problem(np.float32, steps)
         p.flags = flags
         x = DeviceArray.zeros((N * C,), np.float32)
@@ -215,9 +217,10 @@ def test_vectorised_and_scalar_fp32_kernels_agree(dims, C, huber, steps):
         _lib.call("opyx_rof_gap", p, b, stream_ptr())
         off = _lib.load().opyx_rof_info_offset() // 8
         out.append((x.get(), y.get(), ws[off:off + 6].get()))
-    (x0, y0, g0), (x1, y1, g1) = out
-    assert rel(x0, x1) <= 1e-6 and rel(y0, y1) <= 1e-6
-    assert abs(g0[5] - g1[5]) <= 1e-6 * max(1.0, abs(g1[5]))
+    (x0, y0, g0), (x1, y1, g1), (x2, y2, g2) = out
+    for xa, ya, ga in ((x1, y1, g1), (x2, y2, g2)):
+        assert rel(x0, xa) <= 1e-6 and rel(y0, ya) <= 1e-6
+        assert abs(g0[5] - ga[5]) <= 1e-6 * max(1.0, abs(ga[5]))
     Fo = oracle.HuberL1Norms(N, (C, D), 0.07, huber) if huber > 0 else oracle.L1Norms(N, (C, D), 0.07)
     so = oracle.PDHG(oracle.SSD(f.reshape(N, C)), Fo, oracle.Gradient(dims, C, "forward"))
     so.solve(steps=steps, term_pd_gap=1e-300, term_maxiter=iters, granularity=iters,
