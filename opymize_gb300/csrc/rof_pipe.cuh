@@ -135,44 +135,49 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
       pipe_row_coords<D>(g, r, &crow, &cz);
       const bool has_next = crow < g.n[D - 2] - 1;
       const bool has_z = D == 3 && cz < g.n[0] - 1;
+      // this thread's quad, pulled from the slots with 128-bit shared loads
+      float qx[4 * C], qn[4 * C], qz[4 * C], qy[4 * M], xr[C];
+      ldv(qx, xc + lp0 * C);
+      ldv(qn, xn + lp0 * C);
+      if (D == 3) ldv(qz, xz + lp0 * C);
+      ldv(qy, yv + lp0 * M);
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) xr[k2] = xc[(lp0 + 4) * C + k2];
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
-        const int lp = lp0 + p;
-        const int64_t q = q_beg + lp;
+        const int64_t q = q_beg + lp0 + p;
         const bool inx = q < g.nl - 1;
-        float yy[M], sg[M];
-#pragma unroll
-        for (int j = 0; j < M; ++j) yy[j] = yv[lp * M + j];
+        float sg[M];
 #pragma unroll
         for (int k2 = 0; k2 < C; ++k2) {
-          const float xk = xc[lp * C + k2];
-          const float gl = inx ? g.coef[D - 1][k2] * (xc[(lp + 1) * C + k2] - xk) : 0.f;
+          const float xk = qx[p * C + k2];
+          const float nb = p < 3 ? qx[(p + 1) * C + k2] : xr[k2];
+          const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
           sg[(D - 1) * C + k2] = pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c;
-          yy[(D - 1) * C + k2] += sg[(D - 1) * C + k2] * gl;
-          const float gr = has_next ? g.coef[D - 2][k2] * (xn[lp * C + k2] - xk) : 0.f;
+          qy[p * M + (D - 1) * C + k2] += sg[(D - 1) * C + k2] * gl;
+          const float gr = has_next ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
           sg[(D - 2) * C + k2] = pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c;
-          yy[(D - 2) * C + k2] += sg[(D - 2) * C + k2] * gr;
+          qy[p * M + (D - 2) * C + k2] += sg[(D - 2) * C + k2] * gr;
           if (D == 3) {
-            const float gz = has_z ? g.coef[0][k2] * (xz[lp * C + k2] - xk) : 0.f;
+            const float gz = has_z ? g.coef[0][k2] * (qz[p * C + k2] - xk) : 0.f;
             sg[k2] = pre ? (has_z ? g.sig_pre[0][k2] : 0.f) : sig_c;
-            yy[k2] += sg[k2] * gz;
+            qy[p * M + k2] += sg[k2] * gz;
           }
         }
         if (g.use_huber) {
 #pragma unroll
-          for (int j = 0; j < M; ++j) yy[j] /= 1.f + sg[j] * g.hub_ratio;
+          for (int j = 0; j < M; ++j) qy[p * M + j] /= 1.f + sg[j] * g.hub_ratio;
         }
         float n2 = 0.f;
 #pragma unroll
-        for (int j = 0; j < M; ++j) n2 += yy[j] * yy[j];
+        for (int j = 0; j < M; ++j) n2 += qy[p * M + j] * qy[p * M + j];
         if (n2 > g.lbd2) {
           const float sc = g.lbd / sqrtf(n2);
 #pragma unroll
-          for (int j = 0; j < M; ++j) yy[j] *= sc;
+          for (int j = 0; j < M; ++j) qy[p * M + j] *= sc;
         }
-#pragma unroll
-        for (int j = 0; j < M; ++j) yv[lp * M + j] = yy[j];
       }
+      stv(yv + lp0 * M, qy);
       __syncthreads();
       store_row<M, 0>(a.y, yv, g, r, q_beg);
       __syncthreads();
@@ -230,25 +235,33 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
       unsigned mk = 0xffffffffu;
       const int64_t qt = q_beg + lp0;
       if (a.mask && qt < g.nl) mk = *reinterpret_cast<const unsigned*>(a.mask + r * g.nl + qt);
+      // this thread's quad (y slots carry 4 halo pixels on the left)
+      float qy[4 * M], qu[4 * M], qx[4 * C], qf[4 * C], qb[4 * C], yl[C];
+      ldv(qy, yc + (lp0 + 4) * M);
+      ldv(qu, yu + (lp0 + 4) * M);
+      ldv(qx, xv + lp0 * C);
+      ldv(qf, fv + lp0 * C);
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) yl[k2] = yc[(lp0 + 3) * M + (D - 1) * C + k2];
+      float qz[4 * M];
+      if (D == 3) ldv(qz, yz + lp0 * M);
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
-        const int lp = lp0 + p;
-        const int ly = lp + 4;                      // index in the halo slots
-        const int64_t q = q_beg + lp;
+        const int64_t q = q_beg + lp0 + p;
         const bool on = (mk >> (8 * p)) & 0xffu;
 #pragma unroll
         for (int k2 = 0; k2 < C; ++k2) {
           float s = 0.f;
           const float ihl = g.invh[D - 1];
-          if (q < g.nl - 1) s -= yc[ly * M + (D - 1) * C + k2] * ihl;
-          if (q > 0) s += yc[(ly - 1) * M + (D - 1) * C + k2] * ihl;
+          if (q < g.nl - 1) s -= qy[p * M + (D - 1) * C + k2] * ihl;
+          if (q > 0) s += (p > 0 ? qy[(p - 1) * M + (D - 1) * C + k2] : yl[k2]) * ihl;
           const float ihr = g.invh[D - 2];
-          if (has_dn) s -= yc[ly * M + (D - 2) * C + k2] * ihr;
-          if (has_up) s += yu[ly * M + (D - 2) * C + k2] * ihr;
+          if (has_dn) s -= qy[p * M + (D - 2) * C + k2] * ihr;
+          if (has_up) s += qu[p * M + (D - 2) * C + k2] * ihr;
           if (D == 3) {
             const float ihz = g.invh[0];
-            if (has_zf) s -= yc[ly * M + k2] * ihz;
-            if (has_zb) s += yz[lp * M + k2] * ihz;
+            if (has_zf) s -= qy[p * M + k2] * ihz;
+            if (has_zb) s += qz[p * M + k2] * ihz;
           }
           const float dv = g.w[k2] * s;
           float tau = tau_c;
@@ -258,13 +271,15 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
             if (D == 3) cs += g.absc[0][k2] * (float)(has_zf + has_zb);
             tau = cs > 2.220446049250313e-16f ? 1.f / cs : 0.f;
           }
-          const float xo = xv[lp * C + k2];
+          const float xo = qx[p * C + k2];
           float v = xo - tau * dv;
-          if (on) v = ssd_prox_value(v, fv[lp * C + k2], tau * g.vol[k2]);
-          xv[lp * C + k2] = v;
-          bs[lp * C + k2] = g.theta1 * v - g.theta * xo;
+          if (on) v = ssd_prox_value(v, qf[p * C + k2], tau * g.vol[k2]);
+          qx[p * C + k2] = v;
+          qb[p * C + k2] = g.theta1 * v - g.theta * xo;
         }
       }
+      stv(xv + lp0 * C, qx);
+      stv(bs + lp0 * C, qb);
       __syncthreads();
       store_row<C, 0>(a.x, xv, g, r, q_beg);
       store_row<C, 0>(a.xbar, bs, g, r, q_beg);
@@ -335,28 +350,44 @@ __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float
       unsigned mk = 0xffffffffu;
       const int64_t qt = q_beg + lp0;
       if (a.mask && qt < g.nl) mk = *reinterpret_cast<const unsigned*>(a.mask + r * g.nl + qt);
+      // this thread's quad from the slots (128-bit shared loads)
+      float qx[4 * C], qn[4 * C], qf[4 * C], qy[4 * M], qu[4 * M], xr[C], yl[C];
+      float qxz[4 * C], qyz[4 * M];
+      ldv(qx, xc + lp0 * C);
+      ldv(qn, xn + lp0 * C);
+      ldv(qf, fv + lp0 * C);
+      ldv(qy, yc + (lp0 + 4) * M);
+      ldv(qu, yu + (lp0 + 4) * M);
+      if (D == 3) {
+        ldv(qxz, xz + lp0 * C);
+        ldv(qyz, yz + lp0 * M);
+      }
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) {
+        xr[k2] = xc[(lp0 + 4) * C + k2];
+        yl[k2] = yc[(lp0 + 3) * M + (D - 1) * C + k2];
+      }
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
-        const int lp = lp0 + p, ly = lp + 4;
-        const int64_t q = q_beg + lp;
+        const int64_t q = q_beg + lp0 + p;
         if (q >= g.nl) continue;
         const bool on = (mk >> (8 * p)) & 0xffu;
         const bool inx = q < g.nl - 1;
         float n2 = 0.f, y2 = 0.f;
 #pragma unroll
         for (int k2 = 0; k2 < C; ++k2) {
-          const float xk = xc[lp * C + k2], fk = fv[lp * C + k2];
+          const float xk = qx[p * C + k2], fk = qf[p * C + k2];
           // A^T y
           float s = 0.f;
           const float ihl = g.invh[D - 1], ihr = g.invh[D - 2];
-          if (inx) s -= yc[ly * M + (D - 1) * C + k2] * ihl;
-          if (q > 0) s += yc[(ly - 1) * M + (D - 1) * C + k2] * ihl;
-          if (has_dn) s -= yc[ly * M + (D - 2) * C + k2] * ihr;
-          if (has_up) s += yu[ly * M + (D - 2) * C + k2] * ihr;
+          if (inx) s -= qy[p * M + (D - 1) * C + k2] * ihl;
+          if (q > 0) s += (p > 0 ? qy[(p - 1) * M + (D - 1) * C + k2] : yl[k2]) * ihl;
+          if (has_dn) s -= qy[p * M + (D - 2) * C + k2] * ihr;
+          if (has_up) s += qu[p * M + (D - 2) * C + k2] * ihr;
           if (D == 3) {
             const float ihz = g.invh[0];
-            if (has_zf) s -= yc[ly * M + k2] * ihz;
-            if (has_zb) s += yz[lp * M + k2] * ihz;
+            if (has_zf) s -= qy[p * M + k2] * ihz;
+            if (has_zb) s += qyz[p * M + k2] * ihz;
           }
           const float ak = g.w[k2] * s;
           if (on) {
@@ -365,19 +396,17 @@ __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float
             pGs += ak * ak * g.half_rvol[k2] - fk * ak;
           }
           // A x
-          const float gl = inx ? g.coef[D - 1][k2] * (xc[(lp + 1) * C + k2] - xk) : 0.f;
-          const float gr = has_dn ? g.coef[D - 2][k2] * (xn[lp * C + k2] - xk) : 0.f;
+          const float nb = p < 3 ? qx[(p + 1) * C + k2] : xr[k2];
+          const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
+          const float gr = has_dn ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
           n2 += gl * gl + gr * gr;
           if (D == 3) {
-            const float gz = has_zf ? g.coef[0][k2] * (xz[lp * C + k2] - xk) : 0.f;
+            const float gz = has_zf ? g.coef[0][k2] * (qxz[p * C + k2] - xk) : 0.f;
             n2 += gz * gz;
           }
         }
 #pragma unroll
-        for (int j = 0; j < M; ++j) {
-          const float yj = yc[ly * M + j];
-          y2 += yj * yj;
-        }
+        for (int j = 0; j < M; ++j) y2 += qy[p * M + j] * qy[p * M + j];
         const float nrm = sqrtf(n2);
         pF += g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
         pFs += y2;
