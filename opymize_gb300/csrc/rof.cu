@@ -90,6 +90,28 @@ static Geo<T> make_geo(const opyx_rof_problem* p) {
   g.theta = (T)p->theta;
   g.theta1 = (T)(1.0 + p->theta);
   g.steps = p->steps;
+  // preconditioner tables: neighbour counts (n_last, n_row, n_z) -> tau etc.
+  for (int cb = 0; cb < 27; ++cb) {
+    const int nl_ = cb % 3, nr = (cb / 3) % 3, nz = cb / 9;
+    for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
+      const double w = fabs(k < p->nchannels ? p->weights[k] : 1.0);
+      const double v = k < p->nchannels ? p->vol[k] : 1.0;
+      double cs = w * invh[D - 1] * nl_;
+      if (D >= 2) cs += w * invh[D - 2] * nr;
+      if (D == 3) cs += w * invh[0] * nz;
+      const double tau = cs > 2.220446049250313e-16 ? 1.0 / cs : 0.0;
+      g.tau_tab[cb][k] = (T)tau;
+      g.tv_tab[cb][k] = (T)(tau * v);
+      g.a_tab[cb][k] = (T)(1.0 / (1.0 + tau * v));
+    }
+  }
+  for (int t = 0; t < 3; ++t)
+    for (int k = 0; k < OPYX_ROF_MAX_C; ++k) {
+      const double w = k < p->nchannels ? p->weights[k] : 1.0;
+      const double rs = 2.0 * fabs(w) * invh[t];
+      const double sig = rs > 2.220446049250313e-16 ? 1.0 / rs : 0.0;
+      g.hub_pre[t][k] = (T)(1.0 / (1.0 + sig * (p->huber_alpha / p->lbd)));
+    }
   return g;
 }
 

@@ -47,9 +47,40 @@ struct Geo {
   T half_rvol[OPYX_ROF_MAX_C];        // 1/(2 vol_k)
   T lbd, lbd2, hub_ratio, theta, theta1;
   T huber, half_huber, half_rhuber;   // alpha, alpha/2, 1/(2 alpha)
+  // Preconditioned steps depend on a pixel only through how many neighbours
+  // it has along each axis (0, 1 or 2): index cb = n_last + 3 n_row + 9 n_z.
+  T tau_tab[27][OPYX_ROF_MAX_C];      // tau = 1/colsum
+  T a_tab[27][OPYX_ROF_MAX_C];        // 1/(1 + tau vol): SSD prox scale
+  T tv_tab[27][OPYX_ROF_MAX_C];       // tau vol
+  T hub_pre[3][OPYX_ROF_MAX_C];       // 1/(1 + sigma_pre alpha/lbd) on inner rows
   double lbd_d, huber_d;
   int steps;
   bool use_huber;
+};
+
+// Neighbour-count index of the preconditioner tables for a pixel with
+// coordinates c (scalar kernels).
+template <typename T, int D>
+OPYX_D int combo_of(const Geo<T>& g, const int64_t* c) {
+  int cb = (int)((c[D - 1] < g.n[D - 1] - 1) + (c[D - 1] > 0));
+  if (D >= 2) cb += 3 * (int)((c[D - 2] < g.n[D - 2] - 1) + (c[D - 2] > 0));
+  if (D == 3) cb += 9 * (int)((c[0] < g.n[0] - 1) + (c[0] > 0));
+  return cb;
+}
+
+// Primal step coefficients for constant / adaptive steps, computed once per
+// thread: tau, 1/(1 + tau vol_k), tau vol_k.
+template <typename T, int C>
+struct PrimalCoefs {
+  T tau, a[C], tv[C];
+  OPYX_D PrimalCoefs(const Geo<T>& g, T t) {
+    tau = t;
+#pragma unroll
+    for (int k = 0; k < C; ++k) {
+      tv[k] = t * g.vol[k];
+      a[k] = T(1) / (T(1) + tv[k]);
+    }
+  }
 };
 
 // Per-launch constants, by value.
@@ -142,11 +173,13 @@ OPYX_D void grad_at(const Geo<T>& g, const T* __restrict__ v, int64_t i, const i
 
 // prox of sigma*F*: optional Huber shrink y/(1 + sigma*alpha/lbd), then the
 // projection of the D*C group onto the Frobenius ball of radius lbd.
+// hf[j] = 1/(1 + sigma_j alpha/lbd), precomputed (Geo::hub_pre, or once per
+// thread for constant steps).
 template <typename T, int M>
-OPYX_D void fconj_prox(const Geo<T>& g, T (&yv)[M], const T (&sig)[M]) {
+OPYX_D void fconj_prox(const Geo<T>& g, T (&yv)[M], const T (&hf)[M]) {
   if (g.use_huber) {
 #pragma unroll
-    for (int j = 0; j < M; ++j) yv[j] /= T(1) + sig[j] * g.hub_ratio;
+    for (int j = 0; j < M; ++j) yv[j] *= hf[j];
   }
   T nrm = T(0);
 #pragma unroll
@@ -182,7 +215,8 @@ OPYX_D T sigma_const(const Args<T>& a, const Geo<T>& g) {
 template <typename T, int D, int C, int ADAPT>
 __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
   double acc = 0.0;
-  const T tau_c = tau_const(a, g);
+  const PrimalCoefs<T, C> pc(g, tau_const(a, g));
+  const bool pre = g.steps == OPYX_STEPS_PRECOND;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
@@ -195,12 +229,14 @@ __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
       div_at<T, D, C>(g, a.y, i, c, div);
     }
     const bool on = !a.mask || a.mask[i];
+    const int cb = pre ? combo_of<T, D>(g, c) : 0;
 #pragma unroll
     for (int k = 0; k < C; ++k) {
-      const T tau = g.steps == OPYX_STEPS_PRECOND ? precond_tau<T, D>(g, c, k) : tau_c;
+      const T tau = pre ? g.tau_tab[cb][k] : pc.tau;
       const T xo = a.x[i * C + k];
       T xn = xo - tau * div[k];
-      if (on) xn = ssd_prox_value(xn, a.f[i * C + k], tau * g.vol[k]);
+      if (on) xn = (pre ? g.a_tab[cb][k] : pc.a[k]) *
+                   (xn + (pre ? g.tv_tab[cb][k] : pc.tv[k]) * a.f[i * C + k]);
       a.x[i * C + k] = xn;
       a.xbar[i * C + k] = g.theta1 * xn - g.theta * xo;
       if (ADAPT) {
@@ -230,17 +266,21 @@ __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
   constexpr int M = D * C;
   double acc_r = 0.0, acc_g = 0.0;
   const T sig_c = sigma_const(a, g);
+  const T hub_c = T(1) / (T(1) + sig_c * g.hub_ratio);
+  const bool pre = g.steps == OPYX_STEPS_PRECOND;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
     coords<T, D>(g, r, q, c);
-    T gb[M], yv[M], yo[M], sig[M];
+    T gb[M], yv[M], yo[M], sig[M], hf[M];
     grad_at<T, D, C>(g, a.xbar, i, c, gb);
 #pragma unroll
     for (int t = 0; t < D; ++t) {
+      const bool inner = c[t] < g.n[t] - 1;
 #pragma unroll
       for (int k = 0; k < C; ++k) {
-        sig[t * C + k] = g.steps == OPYX_STEPS_PRECOND ? precond_sigma<T, D>(g, c, t, k) : sig_c;
+        sig[t * C + k] = pre ? (inner ? g.sig_pre[t][k] : T(0)) : sig_c;
+        hf[t * C + k] = pre ? (inner ? g.hub_pre[t][k] : T(1)) : hub_c;
       }
     }
 #pragma unroll
@@ -248,7 +288,7 @@ __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
       yo[j] = a.y[i * M + j];
       yv[j] = yo[j] + sig[j] * gb[j];
     }
-    fconj_prox<T, M>(g, yv, sig);
+    fconj_prox<T, M>(g, yv, hf);
 #pragma unroll
     for (int j = 0; j < M; ++j) a.y[i * M + j] = yv[j];
     if (ADAPT) {

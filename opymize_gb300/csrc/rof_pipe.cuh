@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
   const int lp0 = threadIdx.x * 4;         // first local pixel of this thread
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const float sig_c = (float)a.sigma;
+  const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
   const int64_t nplane = D == 3 ? g.n[1] : 0;  // rows per plane
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
@@ -147,26 +148,27 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
       for (int p = 0; p < 4; ++p) {
         const int64_t q = q_beg + lp0 + p;
         const bool inx = q < g.nl - 1;
-        float sg[M];
+        float hf[M];
 #pragma unroll
         for (int k2 = 0; k2 < C; ++k2) {
           const float xk = qx[p * C + k2];
           const float nb = p < 3 ? qx[(p + 1) * C + k2] : xr[k2];
           const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
-          sg[(D - 1) * C + k2] = pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c;
-          qy[p * M + (D - 1) * C + k2] += sg[(D - 1) * C + k2] * gl;
+          qy[p * M + (D - 1) * C + k2] += (pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c) * gl;
+          hf[(D - 1) * C + k2] = pre ? (inx ? g.hub_pre[D - 1][k2] : 1.f) : hub_c;
           const float gr = has_next ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
-          sg[(D - 2) * C + k2] = pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c;
-          qy[p * M + (D - 2) * C + k2] += sg[(D - 2) * C + k2] * gr;
+          qy[p * M + (D - 2) * C + k2] +=
+              (pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c) * gr;
+          hf[(D - 2) * C + k2] = pre ? (has_next ? g.hub_pre[D - 2][k2] : 1.f) : hub_c;
           if (D == 3) {
             const float gz = has_z ? g.coef[0][k2] * (qz[p * C + k2] - xk) : 0.f;
-            sg[k2] = pre ? (has_z ? g.sig_pre[0][k2] : 0.f) : sig_c;
-            qy[p * M + k2] += sg[k2] * gz;
+            qy[p * M + k2] += (pre ? (has_z ? g.sig_pre[0][k2] : 0.f) : sig_c) * gz;
+            hf[k2] = pre ? (has_z ? g.hub_pre[0][k2] : 1.f) : hub_c;
           }
         }
         if (g.use_huber) {
 #pragma unroll
-          for (int j = 0; j < M; ++j) qy[p * M + j] /= 1.f + sg[j] * g.hub_ratio;
+          for (int j = 0; j < M; ++j) qy[p * M + j] *= hf[j];
         }
         float n2 = 0.f;
 #pragma unroll
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
   const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
   const int lp0 = threadIdx.x * 4;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
-  const float tau_c = (float)a.tau;
+  const PrimalCoefs<float, C> pc(g, (float)a.tau);
   const int64_t nplane = D == 3 ? g.n[1] : 0;
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
@@ -249,6 +251,8 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
       for (int p = 0; p < 4; ++p) {
         const int64_t q = q_beg + lp0 + p;
         const bool on = (mk >> (8 * p)) & 0xffu;
+        const int cb = (int)((q < g.nl - 1) + (q > 0)) + 3 * (int)(has_dn + has_up) +
+                       (D == 3 ? 9 * (int)(has_zf + has_zb) : 0);
 #pragma unroll
         for (int k2 = 0; k2 < C; ++k2) {
           float s = 0.f;
@@ -264,16 +268,11 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
             if (has_zb) s += qz[p * M + k2] * ihz;
           }
           const float dv = g.w[k2] * s;
-          float tau = tau_c;
-          if (pre) {
-            float cs = g.absc[D - 1][k2] * (float)((q < g.nl - 1) + (q > 0)) +
-                       g.absc[D - 2][k2] * (float)(has_dn + has_up);
-            if (D == 3) cs += g.absc[0][k2] * (float)(has_zf + has_zb);
-            tau = cs > 2.220446049250313e-16f ? 1.f / cs : 0.f;
-          }
+          const float tau = pre ? g.tau_tab[cb][k2] : pc.tau;
           const float xo = qx[p * C + k2];
           float v = xo - tau * dv;
-          if (on) v = ssd_prox_value(v, qf[p * C + k2], tau * g.vol[k2]);
+          if (on) v = (pre ? g.a_tab[cb][k2] : pc.a[k2]) *
+                      (v + (pre ? g.tv_tab[cb][k2] : pc.tv[k2]) * qf[p * C + k2]);
           qx[p * C + k2] = v;
           qb[p * C + k2] = g.theta1 * v - g.theta * xo;
         }

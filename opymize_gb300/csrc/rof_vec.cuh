@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<floa
   const int lane = threadIdx.x & 31;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const float sig_c = (float)a.sigma;
+  const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
   for (int64_t r0 = blockIdx.y * (int64_t)R; r0 < g.rows; r0 += (int64_t)gridDim.y * R) {
     const int64_t rend = r0 + R < g.rows ? r0 + R : g.rows;
     float xc[4 * C];
@@ -96,28 +97,29 @@ __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<floa
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
         const bool inx = q0 + p < g.nl - 1;
-        float sg[M];
+        float hf[M];
 #pragma unroll
         for (int k = 0; k < C; ++k) {
           const float xk = xc[p * C + k];
           const float nb = p < 3 ? xc[(p + 1) * C + k] : xr[k];
           const float gl = inx ? g.coef[D - 1][k] * (nb - xk) : 0.f;
-          sg[(D - 1) * C + k] = pre ? (inx ? g.sig_pre[D - 1][k] : 0.f) : sig_c;
-          yv[p * M + (D - 1) * C + k] += sg[(D - 1) * C + k] * gl;
+          yv[p * M + (D - 1) * C + k] += (pre ? (inx ? g.sig_pre[D - 1][k] : 0.f) : sig_c) * gl;
+          hf[(D - 1) * C + k] = pre ? (inx ? g.hub_pre[D - 1][k] : 1.f) : hub_c;
           if (D >= 2) {
             const float gr = has_next ? g.coef[D - 2][k] * (xn[p * C + k] - xk) : 0.f;
-            sg[(D - 2) * C + k] = pre ? (has_next ? g.sig_pre[D - 2][k] : 0.f) : sig_c;
-            yv[p * M + (D - 2) * C + k] += sg[(D - 2) * C + k] * gr;
+            yv[p * M + (D - 2) * C + k] +=
+                (pre ? (has_next ? g.sig_pre[D - 2][k] : 0.f) : sig_c) * gr;
+            hf[(D - 2) * C + k] = pre ? (has_next ? g.hub_pre[D - 2][k] : 1.f) : hub_c;
           }
           if (D == 3) {
             const float gz = has_z ? g.coef[0][k] * (xz[p * C + k] - xk) : 0.f;
-            sg[k] = pre ? (has_z ? g.sig_pre[0][k] : 0.f) : sig_c;
-            yv[p * M + k] += sg[k] * gz;
+            yv[p * M + k] += (pre ? (has_z ? g.sig_pre[0][k] : 0.f) : sig_c) * gz;
+            hf[k] = pre ? (has_z ? g.hub_pre[0][k] : 1.f) : hub_c;
           }
         }
         if (g.use_huber) {
 #pragma unroll
-          for (int j = 0; j < M; ++j) yv[p * M + j] /= 1.f + sg[j] * g.hub_ratio;
+          for (int j = 0; j < M; ++j) yv[p * M + j] *= hf[j];
         }
         float n2 = 0.f;
 #pragma unroll
@@ -195,12 +197,14 @@ OPYX_D void quad_back(const Geo<float>& g, const float* __restrict__ y, bool act
   }
 }
 
+// Index of the preconditioner tables for the pixel at last-axis coordinate
+// cl in a row with coordinates (crow, cz).
 template <int D>
-OPYX_D float quad_tau(const Geo<float>& g, int64_t cl, int64_t crow, int64_t cz, int k) {
-  float cs = g.absc[D - 1][k] * (float)((cl < g.nl - 1) + (cl > 0));
-  if (D >= 2) cs += g.absc[D - 2][k] * (float)((crow < g.n[D - 2] - 1) + (crow > 0));
-  if (D == 3) cs += g.absc[0][k] * (float)((cz < g.n[0] - 1) + (cz > 0));
-  return cs > 2.220446049250313e-16f ? 1.f / cs : 0.f;
+OPYX_D int quad_combo(const Geo<float>& g, int64_t cl, int64_t crow, int64_t cz) {
+  int cb = (int)((cl < g.nl - 1) + (cl > 0));
+  if (D >= 2) cb += 3 * (int)((crow < g.n[D - 2] - 1) + (crow > 0));
+  if (D == 3) cb += 9 * (int)((cz < g.n[0] - 1) + (cz > 0));
+  return cb;
 }
 
 // ------------------------------------------------------------------ pass A
@@ -214,7 +218,7 @@ __global__ void __launch_bounds__(kVecThreads) k_passA_v(Geo<float> g, Args<floa
   const int64_t q0 = quad * 4;
   const int lane = threadIdx.x & 31;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
-  const float tau_c = (float)a.tau;
+  const PrimalCoefs<float, C> pc(g, (float)a.tau);
   for (int64_t r0 = blockIdx.y * (int64_t)R; r0 < g.rows; r0 += (int64_t)gridDim.y * R) {
     const int64_t rend = r0 + R < g.rows ? r0 + R : g.rows;
     float yup[4 * C];
@@ -246,11 +250,13 @@ __global__ void __launch_bounds__(kVecThreads) k_passA_v(Geo<float> g, Args<floa
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
           const bool on = (mk >> (8 * p)) & 0xffu;
+          const int cb = pre ? quad_combo<D>(g, q0 + p, crow, cz) : 0;
 #pragma unroll
           for (int k = 0; k < C; ++k) {
-            const float tau = pre ? quad_tau<D>(g, q0 + p, crow, cz, k) : tau_c;
+            const float tau = pre ? g.tau_tab[cb][k] : pc.tau;
             float v = xo[p * C + k] - tau * dv[p * C + k];
-            if (on) v = ssd_prox_value(v, fv[p * C + k], tau * g.vol[k]);
+            if (on) v = (pre ? g.a_tab[cb][k] : pc.a[k]) *
+                        (v + (pre ? g.tv_tab[cb][k] : pc.tv[k]) * fv[p * C + k]);
             xn[p * C + k] = v;
             xb[p * C + k] = g.theta1 * v - g.theta * xo[p * C + k];
           }
