@@ -161,26 +161,22 @@ class ResidentSolver(object):
         b = _lib.opyx_rof_buffers()
         b.x, b.xbar, b.y, b.f, b.ws = self.x.ptr, self.xbar.ptr, self.y.ptr, self.f.ptr, self.ws.ptr
         self.b = b
-        self.info_off = _lib.load().opyx_rof_info_offset() // 8
-        from opymize_gb300.solvers.pdhg import _RofGraph
-        self.graph = _RofGraph(self.p, self.b, self.gran)
+        self.p.term_mode = 1
+        self.p.term_relgap = self.p.term_infeas = self.tol
+        from opymize_gb300.solvers.pdhg import _FusedLoop
+        self.loop = _FusedLoop(self.p, self.b, self.ws, self.gran)
         self.launches = 0
 
     def solve(self, maxiter=5000):
+        """The solver's own check loop (chunks queued ahead of their checks,
+        device-side stop test) from a zero start."""
         from opymize_gb300.gpuarray import stream_ptr
-        L = self.lib
         self.x.fill(0.0)
         self.y.fill(0.0)
-        L.call("opyx_rof_init", self.p, self.b, stream_ptr())
-        self.launches += 3
-        it = 0
-        while it < maxiter:
-            self.graph.launch()
-            self.launches += 2 * self.gran + 1
-            it += self.gran
-            rec = self.ws[self.info_off:self.info_off + 6].get()
-            if abs(rec[5]) < self.tol and max(rec[2], rec[3]) < self.tol:
-                break
+        self.lib.call("opyx_rof_init", self.p, self.b, stream_ptr())
+        l0 = self.loop.launches
+        it, rec = self.loop.run(maxiter)
+        self.launches += 3 + self.loop.launches - l0
         self.iters, self.relgap = it, float(rec[5])
         return it
 
@@ -188,6 +184,8 @@ class ResidentSolver(object):
         from opymize_gb300.gpuarray import torch, stream_ptr
         t = torch()
         s = t.cuda.current_stream()
+        # clears the stop flag of the last solve (the passes would return at once)
+        self.lib.call("opyx_rof_init", self.p, self.b, stream_ptr())
         for _ in range(3):
             self.lib.call("opyx_rof_pass", self.p, self.b, which, stream_ptr())
         e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)

@@ -295,12 +295,19 @@ typedef struct {
   double theta;                     /* overrelaxation (the reference uses 1) */
   double alpha0, eta, Delta;        /* adaptive rule (0.5, 0.95, 1.5)        */
   double eps[4];                    /* adaptive tolerances (pdhg.py:275-280) */
+  double term_relgap;               /* device-side stop test of opyx_rof_gap:  */
+  double term_infeas;               /*   term_mode 1: |relgap| < term_relgap and
+                                         max(infeasp, infeasd) < term_infeas;
+                                       term_mode 2: resp < epsp, resd < epsd
+                                         (adaptive steps)                   */
+  int32_t term_mode;                /* 0: no device-side stop               */
   int32_t rows_per_thread;          /* tile height of the vectorised FP32
                                        kernels; 0 = automatic               */
   int32_t flags;                    /* bit 0: never use the vectorised FP32
                                        kernels; bit 1: never use the
                                        row-streaming FP32 kernels (both for
                                        cross-checks)                        */
+  int32_t reserved;
 } opyx_rof_problem;
 
 typedef struct {
@@ -316,10 +323,15 @@ typedef struct {
                            first use                                         */
 } opyx_rof_buffers;
 
-/* Values of the last opyx_rof_gap (pdhg.py:23-44) and of the step state. */
+/* Values of the last opyx_rof_gap (pdhg.py:23-44) and of the step state.
+ * `checks` counts the gap evaluations since opyx_rof_init; `done` becomes 1
+ * at the first one that passes the stop test of the problem's term_mode,
+ * after which every opyx_rof_* kernel returns at once (so the host may queue
+ * iterations ahead of its checks). */
 typedef struct {
   double objp, objd, infeasp, infeasd, gap, relgap;
   double tau, sigma, alpha, resp, resd, epsp, epsd;
+  double checks, done;
 } opyx_rof_info;
 
 size_t opyx_rof_workspace_size(void);

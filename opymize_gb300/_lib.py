@@ -72,8 +72,10 @@ class opyx_rof_problem(C.Structure):
                 ("ssd_shift", C.c_double), ("lbd", C.c_double), ("huber_alpha", C.c_double),
                 ("tau", C.c_double), ("sigma", C.c_double), ("theta", C.c_double),
                 ("alpha0", C.c_double), ("eta", C.c_double), ("Delta", C.c_double),
-                ("eps", C.c_double * 4), ("rows_per_thread", C.c_int32),
-                ("flags", C.c_int32)]
+                ("eps", C.c_double * 4), ("term_relgap", C.c_double),
+                ("term_infeas", C.c_double), ("term_mode", C.c_int32),
+                ("rows_per_thread", C.c_int32), ("flags", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class opyx_rof_buffers(C.Structure):
@@ -85,7 +87,10 @@ class opyx_rof_buffers(C.Structure):
 class opyx_rof_info(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("objp", "objd", "infeasp", "infeasd", "gap", "relgap", "tau", "sigma",
-                 "alpha", "resp", "resd", "epsp", "epsd")]
+                 "alpha", "resp", "resd", "epsp", "epsd", "checks", "done")]
+
+
+ROF_INFO_FIELDS = [n for n, _ in opyx_rof_info._fields_]
 
 
 vp, i32, i64, f64, sz = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_size_t

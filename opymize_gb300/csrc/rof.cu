@@ -35,6 +35,8 @@ static int validate(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   for (int k = 0; k < p->nchannels; ++k)
     if (!(p->vol[k] > 0)) return OPYX_ERR_ARG;
   if (!(p->lbd > 0) || p->huber_alpha < 0 || !(p->theta > 0)) return OPYX_ERR_ARG;
+  if (p->term_mode < 0 || p->term_mode > 2) return OPYX_ERR_ARG;
+  if (p->term_mode == 2 && p->steps != OPYX_STEPS_ADAPTIVE) return OPYX_ERR_ARG;
   if (p->steps != OPYX_STEPS_PRECOND && (!(p->tau > 0) || !(p->sigma > 0))) return OPYX_ERR_ARG;
   if (p->steps == OPYX_STEPS_ADAPTIVE &&
       (!(p->alpha0 > 0) || !(p->alpha0 < 1) || !(p->Delta > 1) || !(p->eta > 0)))
@@ -90,6 +92,9 @@ static Geo<T> make_geo(const opyx_rof_problem* p) {
   g.theta = (T)p->theta;
   g.theta1 = (T)(1.0 + p->theta);
   g.steps = p->steps;
+  g.term_mode = p->term_mode;
+  g.term_relgap = p->term_relgap;
+  g.term_infeas = p->term_infeas;
   // preconditioner tables: neighbour counts (n_last, n_row, n_z) -> tau etc.
   for (int cb = 0; cb < 27; ++cb) {
     const int nl_ = cb % 3, nr = (cb / 3) % 3, nz = cb / 9;

@@ -54,7 +54,9 @@ struct Geo {
   T tv_tab[27][OPYX_ROF_MAX_C];       // tau vol
   T hub_pre[3][OPYX_ROF_MAX_C];       // 1/(1 + sigma_pre alpha/lbd) on inner rows
   double lbd_d, huber_d;
+  double term_relgap, term_infeas;    // device-side stop test (term_mode)
   int steps;
+  int term_mode;
   bool use_huber;
 };
 
@@ -99,6 +101,51 @@ struct Args {
   opyx_rof_info* info;
   double tau, sigma;  // constant steps
 };
+
+// Every fused kernel returns at once once the stop test has passed, so a
+// host may queue iterations beyond its next check without changing the
+// result.  The flag is written only by the last block of a gap kernel, never
+// while another kernel of the same solve runs, so all threads of a launch
+// read the same value.
+template <typename T>
+OPYX_D bool stopped(const Args<T>& a) {
+  return a.info->done != 0.0;
+}
+
+// Objectives of the gap kernels from the block-reduced sums
+// tot = {sum G-terms, sum |Ax|, sum G*-terms, sum |y|^2, max(|y| - lbd)}
+// (pdhg.py:23-44), the step state, the check counter and the stop test of
+// the reference's solve loop (pdhg.py:290-305).
+template <typename T>
+OPYX_D void write_info(const Geo<T>& g, const Args<T>& a, const double* tot, double ssd_shift) {
+  opyx_rof_info* info = a.info;
+  const opyx_adaptive_state* st = a.st;
+  const double Gx = tot[0] + ssd_shift;
+  const double FAx = g.lbd_d * tot[1];
+  const double Gs = tot[2] - ssd_shift;
+  const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
+  info->objp = Gx + FAx;
+  info->objd = -Gs - Fs;
+  info->infeasp = 0.0;
+  info->infeasd = fmax(0.0, tot[4]);
+  info->gap = info->objp - info->objd;
+  info->relgap = info->gap / fmax(2.220446049250313e-16, fabs(info->objd));
+  info->tau = st->tau;
+  info->sigma = st->sigma;
+  info->alpha = st->alpha;
+  info->resp = st->resp;
+  info->resd = st->resd;
+  info->epsp = st->epsp;
+  info->epsd = st->epsd;
+  info->checks += 1.0;
+  bool stop = false;
+  if (g.term_mode == 1)
+    stop = fabs(info->relgap) < g.term_relgap &&
+           fmax(info->infeasp, info->infeasd) < g.term_infeas;
+  else if (g.term_mode == 2)
+    stop = st->resp < st->epsp && st->resd < st->epsd;
+  if (stop) info->done = 1.0;
+}
 
 // Coordinates of pixel (row r, column q): c[D-1] = q, the others from r.
 template <typename T, int D>
@@ -214,6 +261,7 @@ OPYX_D T sigma_const(const Args<T>& a, const Geo<T>& g) {
 //            gp = (x_k - x_{k+1})/tau - A^T y_k; reduces |gp|^2 into sums[1].
 template <typename T, int D, int C, int ADAPT>
 __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
+  if (stopped(a)) return;
   double acc = 0.0;
   const PrimalCoefs<T, C> pc(g, tau_const(a, g));
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
@@ -263,6 +311,7 @@ __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
 //            into sums[2], sums[3]  (pdhg.py:157-162).
 template <typename T, int D, int C, int ADAPT>
 __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
+  if (stopped(a)) return;
   constexpr int M = D * C;
   double acc_r = 0.0, acc_g = 0.0;
   const T sig_c = sigma_const(a, g);
@@ -323,6 +372,7 @@ __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
 // |r_p|^2 = |gp + A^T y_{k+1}|^2 into sums[0] and applies the step rule.
 template <typename T, int D, int C, int RESID>
 __global__ void __launch_bounds__(256) k_passR(Geo<T> g, Args<T> a) {
+  if (stopped(a)) return;
   double acc = 0.0;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
@@ -357,6 +407,7 @@ __global__ void __launch_bounds__(256) k_passR(Geo<T> g, Args<T> a) {
 // cancellation of its two large sums.
 template <typename T, int D, int C>
 __global__ void __launch_bounds__(256) k_gap(Geo<T> g, Args<T> a, double ssd_shift) {
+  if (stopped(a)) return;
   constexpr int M = D * C;
   double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
   ROF_PIXEL_LOOP {
@@ -398,26 +449,8 @@ __global__ void __launch_bounds__(256) k_gap(Geo<T> g, Args<T> a, double ssd_shi
   }
   double vals[5] = {sG, sF, sGs, sFs, inf};
   const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
-  opyx_rof_info* info = a.info;
-  const opyx_adaptive_state* st = a.st;
   block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
-    const double Gx = tot[0] + ssd_shift;
-    const double FAx = g.lbd_d * tot[1];
-    const double Gs = tot[2] - ssd_shift;
-    const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
-    info->objp = Gx + FAx;
-    info->objd = -Gs - Fs;
-    info->infeasp = 0.0;
-    info->infeasd = fmax(0.0, tot[4]);
-    info->gap = info->objp - info->objd;
-    info->relgap = info->gap / fmax(2.220446049250313e-16, fabs(info->objd));
-    info->tau = st->tau;
-    info->sigma = st->sigma;
-    info->alpha = st->alpha;
-    info->resp = st->resp;
-    info->resd = st->resd;
-    info->epsp = st->epsp;
-    info->epsd = st->epsd;
+    write_info(g, a, tot, ssd_shift);
   });
 }
 

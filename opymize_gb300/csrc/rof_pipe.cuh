@@ -98,6 +98,7 @@ struct PipeSmem {
 // ------------------------------------------------------------------ pass B
 template <int D, int C>
 __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<float> a, int RB) {
+  if (stopped(a)) return;
   using S = PipeSmem<D, C>;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
 #pragma unroll
         for (int j = 0; j < M; ++j) n2 += qy[p * M + j] * qy[p * M + j];
         if (n2 > g.lbd2) {
-          const float sc = g.lbd / sqrtf(n2);
+          const float sc = g.lbd * rsqrtf(n2);   // 2-ulp reciprocal square root
 #pragma unroll
           for (int j = 0; j < M; ++j) qy[p * M + j] *= sc;
         }
@@ -192,6 +193,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
 // ------------------------------------------------------------------ pass A
 template <int D, int C>
 __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<float> a, int RB) {
+  if (stopped(a)) return;
   using S = PipeSmem<D, C>;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
@@ -295,6 +297,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
 template <int D, int C>
 __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float> a, int RB,
                                                         double ssd_shift) {
+  if (stopped(a)) return;
   using S = PipeSmem<D, C>;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
@@ -423,26 +426,8 @@ __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float
   }
   double vals[5] = {sG, sF, sGs, sFs, inf};
   const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
-  opyx_rof_info* info = a.info;
-  const opyx_adaptive_state* st = a.st;
   block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
-    const double Gx = tot[0] + ssd_shift;
-    const double FAx = g.lbd_d * tot[1];
-    const double Gs = tot[2] - ssd_shift;
-    const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
-    info->objp = Gx + FAx;
-    info->objd = -Gs - Fs;
-    info->infeasp = 0.0;
-    info->infeasd = fmax(0.0, tot[4]);
-    info->gap = info->objp - info->objd;
-    info->relgap = info->gap / fmax(2.220446049250313e-16, fabs(info->objd));
-    info->tau = st->tau;
-    info->sigma = st->sigma;
-    info->alpha = st->alpha;
-    info->resp = st->resp;
-    info->resd = st->resd;
-    info->epsp = st->epsp;
-    info->epsd = st->epsd;
+    write_info(g, a, tot, ssd_shift);
   });
 }
 

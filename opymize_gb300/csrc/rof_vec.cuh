@@ -63,6 +63,7 @@ OPYX_D void row_coords(const Geo<float>& g, int64_t r, int64_t* crow, int64_t* c
 // y <- prox_{sigma F*}(y + sigma * A xbar) for R rows of one quad.
 template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<float> a, int R) {
+  if (stopped(a)) return;
   constexpr int M = D * C;
   const int64_t Q = g.nl >> 2;
   const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(kVecThreads) k_passB_v(Geo<float> g, Args<floa
 #pragma unroll
         for (int j = 0; j < M; ++j) n2 += yv[p * M + j] * yv[p * M + j];
         if (n2 > g.lbd2) {
-          const float sc = g.lbd / sqrtf(n2);
+          const float sc = g.lbd * rsqrtf(n2);   // 2-ulp reciprocal square root
 #pragma unroll
           for (int j = 0; j < M; ++j) yv[p * M + j] *= sc;
         }
@@ -211,6 +212,7 @@ OPYX_D int quad_combo(const Geo<float>& g, int64_t cl, int64_t crow, int64_t cz)
 // x <- prox_{tau G}(x - tau A^T y), xbar <- (1+theta) x_new - theta x_old.
 template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_passA_v(Geo<float> g, Args<float> a, int R) {
+  if (stopped(a)) return;
   constexpr int M = D * C;
   const int64_t Q = g.nl >> 2;
   const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -280,6 +282,7 @@ __global__ void __launch_bounds__(kVecThreads) k_passA_v(Geo<float> g, Args<floa
 template <int D, int C>
 __global__ void __launch_bounds__(kVecThreads) k_gap_v(Geo<float> g, Args<float> a, int R,
                                                        double ssd_shift) {
+  if (stopped(a)) return;
   constexpr int M = D * C;
   const int64_t Q = g.nl >> 2;
   const int64_t quad = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -381,26 +384,8 @@ __global__ void __launch_bounds__(kVecThreads) k_gap_v(Geo<float> g, Args<float>
   }
   double vals[5] = {sG, sF, sGs, sFs, inf};
   const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
-  opyx_rof_info* info = a.info;
-  const opyx_adaptive_state* st = a.st;
   block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
-    const double Gx = tot[0] + ssd_shift;
-    const double FAx = g.lbd_d * tot[1];
-    const double Gs = tot[2] - ssd_shift;
-    const double Fs = g.use_huber ? 0.5 * g.huber_d / g.lbd_d * tot[3] : 0.0;
-    info->objp = Gx + FAx;
-    info->objd = -Gs - Fs;
-    info->infeasp = 0.0;
-    info->infeasd = fmax(0.0, tot[4]);
-    info->gap = info->objp - info->objd;
-    info->relgap = info->gap / fmax(2.220446049250313e-16, fabs(info->objd));
-    info->tau = st->tau;
-    info->sigma = st->sigma;
-    info->alpha = st->alpha;
-    info->resp = st->resp;
-    info->resd = st->resd;
-    info->epsp = st->epsp;
-    info->epsd = st->epsd;
+    write_info(g, a, tot, ssd_shift);
   });
 }
 

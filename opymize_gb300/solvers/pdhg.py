@@ -197,50 +197,31 @@ class PDHG(object):
         b.ws = ws.ptr
         self._fused = dict(x=x, y=y, xbar=xbar, f=fdev, mask=mask, xgrad=xgrad, gp=gp, ws=ws,
                            problem=p, buffers=b)
-        info_off = lib.opyx_rof_info_offset() // 8
-        s = stream_ptr()
-        _lib.call("opyx_rof_init", p, b, s)
-
-        graphs = {}
-
-        def run_chunk(n):
-            if graph:
-                if n not in graphs:
-                    graphs[n] = _RofGraph(p, b, n)
-                graphs[n].launch()
-            else:
-                _lib.call("opyx_rof_iterate", p, b, n, stream_ptr())
-                _lib.call("opyx_rof_gap", p, b, stream_ptr())
-
+        if pd_res_mode:
+            p.term_mode = 2
+        else:
+            p.term_mode = 1
+            p.term_relgap, p.term_infeas = float(term_pd_gap[0]), float(term_pd_gap[1])
+        _lib.call("opyx_rof_init", p, b, stream_ptr())
+        loop = _FusedLoop(p, b, ws, granularity, graph=graph)
+        self._fused['loop'] = loop
         t0 = time.perf_counter()
-        _iter = 0
+
+        def on_check(rec, it):
+            self._record_info(rec, it, t0)
+            if cbfun is not None:
+                self._download(x, y)
+                cbfun(self.state, self.info)
+
+        # a callback sees the state of its own check, so it waits for each
+        depth = 0 if cbfun is not None else _FusedLoop.DEPTH
         with GracefulInterruptHandler() as hdl:
-            while _iter < term_maxiter:
-                n = min(granularity - (_iter % granularity), term_maxiter - _iter)
-                check = (_iter + n) % granularity == 0
-                if check:
-                    run_chunk(n)
-                else:
-                    _lib.call("opyx_rof_iterate", p, b, n, stream_ptr())
-                _iter += n
-                if hdl.interrupted or check:
-                    if not check:
-                        _lib.call("opyx_rof_gap", p, b, stream_ptr())
-                    rec = ws[info_off:info_off + 13].get()
-                    self._record_info(rec, _iter, t0)
-                    if cbfun is not None:
-                        self._download(x, y)
-                        cbfun(self.state, self.info)
-                    if self._check(pd_res_mode, term_pd_gap) or hdl.interrupted:
-                        break
+            it, _ = loop.run(term_maxiter, depth, on_check, lambda: hdl.interrupted)
         self._download(x, y)
-        self.info.setdefault('iter', _iter)
-        self.info['iter'] = _iter
+        self.info['iter'] = it
 
     def _record_info(self, rec, it, t0):
-        names = ("objp", "objd", "infeasp", "infeasd", "gap", "relgap", "tau", "sigma",
-                 "alpha", "resp", "resd", "epsp", "epsd")
-        d = dict(zip(names, (float(v) for v in rec)))
+        d = dict(zip(_lib.ROF_INFO_FIELDS, (float(v) for v in rec)))
         for k in INFO_KEYS:
             self.info[k] = d[k]
         if 'adaptive' in self.constvars:
@@ -392,6 +373,96 @@ class _AdaptiveState(object):
         h = _lib.opyx_adaptive_state.from_buffer_copy(raw.tobytes())
         self.tau.host_value, self.sigma.host_value = h.tau, h.sigma
         return h
+
+
+class _FusedLoop(object):
+    """Fused iterations queued ahead of their checks.
+
+    A check chunk is `granularity` iterations and the gap kernel (one CUDA
+    graph per chunk length), then an asynchronous copy of the info record into
+    a pinned host slot and an event.  The host reads a record only when
+    `depth` newer chunks are queued behind it, so the GPU does not idle on the
+    host round trip.  The device-side stop test (term_mode of the problem)
+    makes every kernel queued after the passing check return at once, so
+    state, info and iteration count equal those of a loop that waits at every
+    check, as the reference's does (opymize/solvers/pdhg.py:285-313).
+    `run` must follow opyx_rof_init, which clears the check counter.
+    """
+    DEPTH = 2
+
+    def __init__(self, p, b, ws, granularity, graph=True):
+        self.p, self.b, self.gran, self.use_graph = p, b, int(granularity), graph
+        off = _lib.load().opyx_rof_info_offset() // 8
+        self.info_dev = ws.t[off:off + len(_lib.ROF_INFO_FIELDS)]
+        self.graphs = {}
+        self.host = None
+        self.launches = 0      # kernel launches queued so far
+
+    def chunk(self, n, check):
+        if check and self.use_graph:
+            g = self.graphs.get(n)
+            if g is None:
+                g = self.graphs[n] = _RofGraph(self.p, self.b, n)
+            g.launch()
+        else:
+            _lib.call("opyx_rof_iterate", self.p, self.b, n, stream_ptr())
+            if check:
+                _lib.call("opyx_rof_gap", self.p, self.b, stream_ptr())
+        per_it = 3 if self.p.steps == _lib.STEPS["adaptive"] else 2
+        self.launches += n * per_it + (1 if check else 0)
+
+    def run(self, maxiter, depth=DEPTH, on_check=None, interrupted=None):
+        """Iterate until the stop test passes at a check, `maxiter` iterations
+        are done or `interrupted()` is true (then the current chunk ends with a
+        check, as the reference's interrupt does).  Calls on_check(record,
+        iteration) for every check that ran, in order; returns (iterations
+        done, last record read)."""
+        t = torch()
+        nrec = len(_lib.ROF_INFO_FIELDS)
+        if self.host is None or self.host.shape[0] < depth + 1:
+            self.host = t.empty((depth + 1, nrec), dtype=t.float64, pin_memory=True)
+        i_checks, i_done = nrec - 2, nrec - 1
+        pending = []          # (event, slot) of queued checks, oldest first
+        check_iters = []      # iteration count at each queued check
+        state = {"rec": None, "checks": 0}
+
+        def read_oldest():
+            ev, slot = pending.pop(0)
+            ev.synchronize()
+            rec = self.host[slot].numpy().copy()
+            c = int(rec[i_checks])
+            if c > state["checks"]:      # checks after the stop returned at once
+                state["checks"], state["rec"] = c, rec
+                if on_check is not None:
+                    on_check(rec, check_iters[c - 1])
+            return rec[i_done] != 0.0
+
+        it, done = 0, False
+        while it < maxiter and not done:
+            n = min(self.gran - (it % self.gran), maxiter - it)
+            it += n
+            stop = interrupted is not None and bool(interrupted())
+            check = it % self.gran == 0 or stop
+            self.chunk(n, check)
+            if check:
+                slot = len(check_iters) % (depth + 1)
+                check_iters.append(it)
+                self.host[slot].copy_(self.info_dev, non_blocking=True)
+                ev = t.cuda.Event()
+                ev.record()
+                pending.append((ev, slot))
+                if len(pending) > depth:
+                    done = read_oldest()
+            if stop:
+                break
+        while pending:
+            done = read_oldest() or done
+        rec = state["rec"]
+        if rec is not None and rec[i_done] != 0.0:
+            it = check_iters[state["checks"] - 1]
+        else:
+            t.cuda.current_stream().synchronize()
+        return it, rec
 
 
 class _RofGraph(object):
