@@ -149,6 +149,40 @@ int opyx_indexedmult_adj(int dtype, int J, int64_t N, int M, int L, int K,
                          const double* B, const int64_t* P, const void* x, void* y,
                          int add, void* stream);
 
+/* ------------------------------------------------ piecewise-linear epigraphs */
+/* Instance (j, i) of x (nregions, nfuns, ndim+1) is constrained by
+ * <v[l], y[:ndim]> - y[ndim] <= b[i, l] for l = J[j, k] (k < nsubpoints) with
+ * I[i, l] != 0: the epigraph of the conjugate of the convex piece j of the
+ * piecewise-linear function i (opymize/operators/proj.py:388-480).  v and b
+ * are in the iterate dtype; the EpigraphSupp value additionally needs the
+ * affine pieces of every instance (eq_off, eqns) and the region checks, both
+ * FP64 (functionals/epigraph.py:56-112). */
+typedef struct {
+  int32_t ndim;               /* 1..3                                       */
+  int32_t nsubpoints;
+  int64_t nfuns, nregions, npoints;
+  const uint8_t* I;           /* (nfuns, npoints)                           */
+  const int64_t* J;           /* (nregions, nsubpoints), values < npoints   */
+  const void* v;              /* (npoints, ndim)                            */
+  const void* b;              /* (nfuns, npoints)                           */
+  const int64_t* eq_off;      /* (nregions*nfuns + 1) row offsets, or NULL  */
+  const double* eqns;         /* (eq_off[last], ndim+1), or NULL            */
+  const double* checks;       /* (nregions, ndim+1, ndim+1), or NULL        */
+} opyx_epigraph;
+
+/* y = EpigraphProj(x) (proj.py:388-480; reference kernel `epigraphproj` with
+ * `solve_qp`, proj.cu:660-831): per-instance active-set QP.  y may equal x.
+ * Instances whose QP did not finish within maxiter steps (the reference uses
+ * ndim*nsubpoints, tolerance 1e-9) are counted into *nonconv (device
+ * unsigned, may be NULL); the reference prints a warning instead. */
+int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y,
+                       int maxiter, double tol, unsigned* nonconv, void* stream);
+/* out (device double[2]) = {val, infeas} of EpigraphInd (which = 0,
+ * epigraph.py:40-46) or EpigraphSupp (which = 1, epigraph.py:101-112) at x,
+ * reduced in FP64; ws as for opyx_fct_eval. */
+int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void* x,
+                       double* out, void* ws, void* stream);
+
 /* ------------------------------------------------------------- step sizes */
 /* A step size is a per-element device vector (`vec`, of the iterate dtype,
  * preconditioned steps), else a device double written by the solver

@@ -65,6 +65,13 @@ class opyx_fct(C.Structure):
                 ("vol", C.c_void_p), ("mask", C.c_void_p)]
 
 
+class opyx_epigraph(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("nsubpoints", C.c_int32), ("nfuns", C.c_int64),
+                ("nregions", C.c_int64), ("npoints", C.c_int64), ("I", C.c_void_p),
+                ("J", C.c_void_p), ("v", C.c_void_p), ("b", C.c_void_p),
+                ("eq_off", C.c_void_p), ("eqns", C.c_void_p), ("checks", C.c_void_p)]
+
+
 class opyx_rof_problem(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("ndim", C.c_int32), ("nchannels", C.c_int32),
                 ("steps", C.c_int32), ("dims", C.c_int64 * 3), ("h", C.c_double * 3),
@@ -135,6 +142,8 @@ SIGNATURES = {
                                  vp, vp, vp]),
     "opyx_adaptive_update": (i32, [vp, vp]),
     "opyx_fct_eval": (i32, [P(opyx_fct), i32, vp, vp, vp, vp]),
+    "opyx_epigraph_proj": (i32, [P(opyx_epigraph), i32, vp, vp, i32, f64, vp, vp]),
+    "opyx_epigraph_eval": (i32, [P(opyx_epigraph), i32, i32, vp, vp, vp, vp]),
     "opyx_rof_workspace_size": (sz, []),
     "opyx_rof_info_offset": (sz, []),
     "opyx_rof_init": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), vp]),

@@ -1,0 +1,356 @@
+// Projection onto epigraphs of piecewise-linear convex conjugates, and the
+// values of EpigraphInd / EpigraphSupp (opymize/operators/proj.py:388-480,
+// proj.cu:222-831; opymize/functionals/epigraph.py:7-127).
+//
+// Instance (j, i) -- region j, function i -- owns the n+1 values x[j, i, :]
+// (n = ndim) and the constraints
+//
+//     <v[l], y[:n]> - y[n] <= b[i, l]   for l = J[j, k] with I[i, l] set,
+//
+// i.e. rows a_l = (v[l], -1).  The projection is a tiny strictly convex QP; it
+// is solved per thread with the primal active-set method (Nocedal & Wright,
+// Numerical Optimization, 2nd ed., Algorithm 16.3), as the reference does.
+// The equality-constrained subproblems and the Lagrange multipliers come from
+// the Gram matrix G = A_W A_W^T of the working set W (|W| <= n+1 <= 4), solved
+// by Gaussian elimination with partial pivoting, for every n alike.
+#include "common.cuh"
+
+namespace opyx {
+namespace epi {
+
+constexpr int kThreads = 128;
+constexpr int kEvalBlocks = 1024;
+
+template <typename T, int ND>
+struct Inst {
+  const T* v;          // (npoints, ND)
+  const T* brow;       // b[i, :]
+  const uint8_t* irow; // I[i, :]
+  const int64_t* jrow; // J[j, :]
+  int nsub;
+};
+
+// a_l . y with a_l = (v[l], -1)
+template <typename T, int ND>
+OPYX_D T adot(const T* vl, const T* y) {
+  T s = -y[ND];
+#pragma unroll
+  for (int k = 0; k < ND; ++k) s += vl[k] * y[k];
+  return s;
+}
+
+// <a_l, a_m> = <v_l, v_m> + 1
+template <typename T, int ND>
+OPYX_D T agram(const T* vl, const T* vm) {
+  T s = T(1);
+#pragma unroll
+  for (int k = 0; k < ND; ++k) s += vl[k] * vm[k];
+  return s;
+}
+
+// Solve G z = r in place (r <- z) for the leading m x m block, m <= NA.
+// Returns false if a pivot is not above `tiny` times the largest diagonal.
+template <typename T, int NA>
+OPYX_D bool gauss_solve(T (&G)[NA][NA], T (&r)[NA], int m) {
+  T scale = T(0);
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+    if (a < m) scale = fmax(scale, fabs(G[a][a]));
+  const T tiny = (sizeof(T) == 4 ? T(1e-6) : T(1e-13)) * scale;
+#pragma unroll
+  for (int c = 0; c < NA; ++c) {
+    if (c >= m) break;
+    int piv = c;
+#pragma unroll
+    for (int a = c + 1; a < NA; ++a)
+      if (a < m && fabs(G[a][c]) > fabs(G[piv][c])) piv = a;
+    if (!(fabs(G[piv][c]) > tiny)) return false;
+    if (piv != c) {
+#pragma unroll
+      for (int q = 0; q < NA; ++q) { T t = G[c][q]; G[c][q] = G[piv][q]; G[piv][q] = t; }
+      T t = r[c]; r[c] = r[piv]; r[piv] = t;
+    }
+    const T inv = T(1) / G[c][c];
+#pragma unroll
+    for (int a = c + 1; a < NA; ++a) {
+      if (a >= m) break;
+      const T f = G[a][c] * inv;
+#pragma unroll
+      for (int q = c; q < NA; ++q) G[a][q] -= f * G[c][q];
+      r[a] -= f * r[c];
+    }
+  }
+#pragma unroll
+  for (int c = NA - 1; c >= 0; --c) {
+    if (c >= m) continue;
+    T s = r[c];
+#pragma unroll
+    for (int q = c + 1; q < NA; ++q)
+      if (q < m) s -= G[c][q] * r[q];
+    r[c] = s / G[c][c];
+  }
+  return true;
+}
+
+// Coefficients z of the least-squares fit A_W^T z ~ d (G z = A_W d).
+template <typename T, int ND>
+OPYX_D bool working_coeffs(const T (&aw)[ND + 1][ND], int m, const T* d, T (&z)[ND + 1]) {
+  constexpr int NA = ND + 1;
+  T G[NA][NA];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) {
+    z[a] = a < m ? adot<T, ND>(aw[a], d) : T(0);
+#pragma unroll
+    for (int c = 0; c < NA; ++c) G[a][c] = (a < m && c < m) ? agram<T, ND>(aw[a], aw[c]) : T(0);
+  }
+  return gauss_solve<T, NA>(G, z, m);
+}
+
+// Projection of one instance.  Returns false when the method did not finish
+// within maxiter steps (the last iterate is kept, as the reference does).
+template <typename T, int ND>
+OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol) {
+  constexpr int N1 = ND + 1, NA = ND + 1;
+  // feasible start: raise the last coordinate by the largest violation
+  T viol = T(0);
+  int first = -1;
+  for (int k = 0; k < in.nsub; ++k) {
+    const int64_t l = in.jrow[k];
+    if (!in.irow[l]) continue;
+    const T r = adot<T, ND>(in.v + l * ND, x) - in.brow[l];
+    if (r > viol) { viol = r; first = (int)l; }
+  }
+#pragma unroll
+  for (int k = 0; k < N1; ++k) y[k] = x[k];
+  if (first < 0) return true;     // feasible points are their own projection
+  y[ND] += viol;
+  int W[NA];
+  T aw[NA][ND];
+  int m = 1;
+  W[0] = first;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) aw[0][k] = in.v[first * ND + k];
+  for (int it = 0; it < maxiter; ++it) {
+    // step: the part of x - y orthogonal to the active normals
+    T d[N1], p[N1], z[NA];
+#pragma unroll
+    for (int k = 0; k < N1; ++k) d[k] = x[k] - y[k];
+    if (!working_coeffs<T, ND>(aw, m, d, z)) return false;
+#pragma unroll
+    for (int k = 0; k < N1; ++k) p[k] = d[k];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+      if (a >= m) break;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) p[k] -= z[a] * aw[a][k];
+      p[ND] += z[a];
+    }
+    T pn = T(0);
+#pragma unroll
+    for (int k = 0; k < N1; ++k) pn += fabs(p[k]);
+    int blocking = -1;
+    if (m < NA && pn > T(0)) {
+      // the nearest constraint outside W that the step would cross
+      T smin = T(1);
+      for (int k = 0; k < in.nsub; ++k) {
+        const int64_t l = in.jrow[k];
+        if (!in.irow[l]) continue;
+        bool act = false;
+#pragma unroll
+        for (int a = 0; a < NA; ++a) act |= (a < m && W[a] == (int)l);
+        if (act) continue;
+        const T* vl = in.v + l * ND;
+        const T ap = adot<T, ND>(vl, p);
+        if (ap > tol) {
+          const T s = (in.brow[l] - adot<T, ND>(vl, y)) / ap;
+          if (s < smin && s > -tol) { smin = s; blocking = (int)l; }
+        }
+      }
+      if (smin != T(0)) {
+#pragma unroll
+        for (int k = 0; k < N1; ++k) y[k] += smin * p[k];
+      }
+    }
+    if (blocking >= 0) {
+      W[m] = blocking;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) aw[m][k] = in.v[blocking * ND + k];
+      ++m;
+      if (m < NA) continue;
+    }
+    // no blocking constraint (or a full working set): multipliers of
+    // x - y = A_W^T lambda decide optimality
+#pragma unroll
+    for (int k = 0; k < N1; ++k) d[k] = x[k] - y[k];
+    if (!working_coeffs<T, ND>(aw, m, d, z)) return false;
+    int amin = -1;
+    T lmin = T(0);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+      if (a < m && z[a] < lmin) { lmin = z[a]; amin = a; }
+    if (amin < 0) return true;   // KKT point of the full problem
+    // drop the most negative multiplier
+    --m;
+    W[amin] = W[m];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) aw[amin][k] = aw[m][k];
+  }
+  return false;
+}
+
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads)
+k_proj(opyx_epigraph e, const T* __restrict__ x, T* y, int maxiter, double tol,
+       unsigned* nonconv) {
+  constexpr int N1 = ND + 1;
+  const int64_t total = e.nregions * e.nfuns;
+  unsigned bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / e.nfuns, i = t - j * e.nfuns;
+    Inst<T, ND> in;
+    in.v = (const T*)e.v;
+    in.brow = (const T*)e.b + i * e.npoints;
+    in.irow = e.I + i * e.npoints;
+    in.jrow = e.J + j * e.nsubpoints;
+    in.nsub = e.nsubpoints;
+    T xi[N1], yi[N1];
+#pragma unroll
+    for (int k = 0; k < N1; ++k) xi[k] = x[t * N1 + k];
+    if (!project<T, ND>(in, xi, yi, maxiter, (T)tol)) ++bad;
+#pragma unroll
+    for (int k = 0; k < N1; ++k) y[t * N1 + k] = yi[k];
+  }
+  if (nonconv && bad) atomicAdd(nonconv, bad);
+}
+
+// which = 0: EpigraphInd (val 0, infeas = max(0, max_l a_l.x - b_l));
+// which = 1: EpigraphSupp (val = sum xt * max_f <eq_f, (x[:n]/xt, 1)>, xt =
+// max(eps, |x[n]|); infeas = max(0, -checks[j] x)) (epigraph.py:40-46, :101-112).
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads)
+k_eval(opyx_epigraph e, int which, const T* __restrict__ x, double* out, double* partials,
+       unsigned* ticket) {
+  constexpr int N1 = ND + 1;
+  const int64_t total = e.nregions * e.nfuns;
+  double val = 0.0, inf = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / e.nfuns, i = t - j * e.nfuns;
+    double xi[N1];
+#pragma unroll
+    for (int k = 0; k < N1; ++k) xi[k] = (double)x[t * N1 + k];
+    if (which == 0) {
+      const T* v = (const T*)e.v;
+      const T* b = (const T*)e.b;
+      for (int k = 0; k < e.nsubpoints; ++k) {
+        const int64_t l = e.J[j * e.nsubpoints + k];
+        if (!e.I[i * e.npoints + l]) continue;
+        double s = -xi[ND];
+#pragma unroll
+        for (int q = 0; q < ND; ++q) s += (double)v[l * ND + q] * xi[q];
+        inf = fmax(inf, s - (double)b[i * e.npoints + l]);
+      }
+    } else {
+      const double* ch = e.checks + j * N1 * N1;
+#pragma unroll
+      for (int r = 0; r < N1; ++r) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < N1; ++q) s += ch[r * N1 + q] * xi[q];
+        inf = fmax(inf, -s);
+      }
+      const double xt = fmax(2.220446049250313e-16, fabs(xi[ND]));
+      double best = -INFINITY;
+      for (int64_t f = e.eq_off[t]; f < e.eq_off[t + 1]; ++f) {
+        const double* eq = e.eqns + f * N1;
+        double s = eq[ND];
+#pragma unroll
+        for (int q = 0; q < ND; ++q) s += eq[q] * (xi[q] / xt);
+        best = fmax(best, s);
+      }
+      if (e.eq_off[t + 1] > e.eq_off[t]) val += xt * best;
+    }
+  }
+  double vals[2] = {val, inf};
+  const int ops[2] = {RED_SUM, RED_MAX};
+  block_reduce_and_finish<2>(vals, ops, partials, ticket, [&](double* tot) {
+    out[0] = which == 0 ? 0.0 : tot[0];
+    out[1] = fmax(0.0, tot[1]);
+  });
+}
+
+static int check(const opyx_epigraph* e) {
+  if (!e || e->ndim < 1 || e->ndim > 3) return OPYX_ERR_UNSUPPORTED;
+  if (e->nfuns < 0 || e->nregions < 0 || e->npoints < 1 || e->nsubpoints < 1)
+    return OPYX_ERR_ARG;
+  if (!e->I || !e->J || !e->v || !e->b) return OPYX_ERR_ARG;
+  return OPYX_OK;
+}
+
+}  // namespace epi
+}  // namespace opyx
+
+using namespace opyx;
+using namespace opyx::epi;
+
+extern "C" {
+
+int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y, int maxiter,
+                       double tol, unsigned* nonconv, void* stream) {
+  int st = check(e);
+  if (st) return st;
+  const int64_t total = e->nregions * e->nfuns;
+  if (total == 0) return OPYX_OK;
+  if (!x || !y || maxiter < 1 || !(tol >= 0)) return OPYX_ERR_ARG;
+  const unsigned g = grid_for(total, kThreads, 16);
+  cudaStream_t s = (cudaStream_t)stream;
+#define OPYX_EPI_LAUNCH(TT, ND)                                                        \
+  k_proj<TT, ND><<<g, kThreads, 0, s>>>(*e, (const TT*)x, (TT*)y, maxiter, tol, nonconv)
+  if (dtype == OPYX_F32) {
+    if (e->ndim == 1) OPYX_EPI_LAUNCH(float, 1);
+    else if (e->ndim == 2) OPYX_EPI_LAUNCH(float, 2);
+    else OPYX_EPI_LAUNCH(float, 3);
+  } else if (dtype == OPYX_F64) {
+    if (e->ndim == 1) OPYX_EPI_LAUNCH(double, 1);
+    else if (e->ndim == 2) OPYX_EPI_LAUNCH(double, 2);
+    else OPYX_EPI_LAUNCH(double, 3);
+  } else {
+    return OPYX_ERR_ARG;
+  }
+#undef OPYX_EPI_LAUNCH
+  return check_launch();
+}
+
+int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void* x,
+                       double* out, void* ws, void* stream) {
+  int st = check(e);
+  if (st) return st;
+  if (which != 0 && which != 1) return OPYX_ERR_ARG;
+  if (which == 1 && (!e->eq_off || !e->eqns || !e->checks)) return OPYX_ERR_ARG;
+  if (!out || !ws || ((uintptr_t)ws & 7)) return OPYX_ERR_WORKSPACE;
+  const int64_t total = e->nregions * e->nfuns;
+  if (total > 0 && !x) return OPYX_ERR_ARG;
+  double* partials = (double*)ws;
+  unsigned* ticket = (unsigned*)((char*)ws + (size_t)kEvalBlocks * 8 * sizeof(double));
+  unsigned g = grid_for(total > 0 ? total : 1, kThreads, 4);
+  if (g > (unsigned)kEvalBlocks) g = kEvalBlocks;
+  cudaStream_t s = (cudaStream_t)stream;
+#define OPYX_EPI_EVAL(TT, ND)                                                          \
+  k_eval<TT, ND><<<g, kThreads, 0, s>>>(*e, which, (const TT*)x, out, partials, ticket)
+  if (dtype == OPYX_F32) {
+    if (e->ndim == 1) OPYX_EPI_EVAL(float, 1);
+    else if (e->ndim == 2) OPYX_EPI_EVAL(float, 2);
+    else OPYX_EPI_EVAL(float, 3);
+  } else if (dtype == OPYX_F64) {
+    if (e->ndim == 1) OPYX_EPI_EVAL(double, 1);
+    else if (e->ndim == 2) OPYX_EPI_EVAL(double, 2);
+    else OPYX_EPI_EVAL(double, 3);
+  } else {
+    return OPYX_ERR_ARG;
+  }
+#undef OPYX_EPI_EVAL
+  return check_launch();
+}
+
+}  // extern "C"

@@ -10,7 +10,9 @@ from opymize_gb300.functionals.l1norms import (L1Norms, L1NormsConj,            
                                                HuberL1Norms, HuberL1NormsConj)
 from opymize_gb300.functionals.epigraph import (QuadEpiInd, QuadEpiSupp,        # noqa: F401
                                                 QuadSupport, HuberPerspective,
-                                                TruncQuadEpiInd, quad_dual_coefficients)
+                                                TruncQuadEpiInd, quad_dual_coefficients,
+                                                EpigraphInd, EpigraphFct, EpigraphSupp,
+                                                EpigraphSupportFct)
 from opymize_gb300.functionals.indicators import (AffineFct, ConstFct, ZeroFct,  # noqa: F401
                                                   MaskedAffineFct, IndicatorFct,
                                                   ConstrainFct, PositivityFct,

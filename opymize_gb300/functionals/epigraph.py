@@ -111,3 +111,104 @@ class TruncQuadEpiInd(Functional):
 
     def prox(self, tau):
         return self._prox
+
+
+def _epigraph_eval(data, which, x, supp=None):
+    from opymize_gb300 import _lib
+    from opymize_gb300.gpuarray import DeviceArray, Workspace, stream_ptr
+    assert x.size == data.nregions * data.nfuns * (data.ndim + 1)
+    ws = Workspace.get(_lib.load().opyx_reduce_workspace_size())
+    out = DeviceArray.zeros((2,), np.float64)
+    _lib.call("opyx_epigraph_eval", data.struct(x.dtype, supp), x.dcode, int(which), x.ptr,
+              out.ptr, ws.ptr, stream_ptr())
+    h = out.get()
+    return float(h[0]), float(h[1])
+
+
+class EpigraphInd(Functional):
+    """F(x) = 0 if <v[k], x[j,i,:-1]> - b[i,k] <= x[j,i,-1] for every i, j and
+    k in J[j] with I[i,k], else inf (opymize/functionals/epigraph.py:7-54).
+    The value is (0, infeasibility) reduced on the device; prox = EpigraphProj
+    (independent of tau)."""
+
+    def __init__(self, I, If, J, v, b, conj=None):
+        from opymize_gb300.operators.proj import EpigraphProj
+        Functional.__init__(self)
+        self._prox = EpigraphProj(I, J, v, b)
+        d = self._prox.data
+        self.I, self.If, self.J, self.v, self.b = d.I, If, d.J, d.v, d.b
+        self.x = Variable((d.nregions, d.nfuns, d.ndim + 1))
+        self.conj = EpigraphSupp(I, If, J, v, b, conj=self) if conj is None else conj
+
+    @property
+    def A(self):
+        return self._prox.Ab[0]
+
+    def _eval_gpu(self, x):
+        return _epigraph_eval(self._prox.data, 0, x)
+
+    def prox(self, tau):
+        return self._prox
+
+
+EpigraphFct = EpigraphInd
+
+
+class EpigraphSupp(Functional):
+    """F(x) = max sum_ji <y, x[j,i]> over y[j,i] in epi(f[i]_j*): the support
+    function of the epigraphs (opymize/functionals/epigraph.py:56-112).
+    f[i]_j is given by its affine faces If[i][j] (rows of ndim+1 indices
+    into J[j]); the face equations and the region checks are computed once on
+    the host, the value is reduced on the device."""
+
+    def __init__(self, I, If, J, v, b, conj=None):
+        from opymize_gb300.operators.proj import _EpigraphData
+        Functional.__init__(self)
+        self.data = _EpigraphData(I, J, v, b)
+        d = self.data
+        self.I, self.If, self.J, self.v, self.b = d.I, If, d.J, d.v, d.b
+        self.x = Variable((d.nregions, d.nfuns, d.ndim + 1))
+        self._pieces = None
+        self._supp_dev = None
+        self.conj = EpigraphInd(I, If, J, v, b, conj=self) if conj is None else conj
+
+    def pieces(self):
+        """(eq_off, eqns, checks): per instance (j, i) the affine functions
+        c.p + d through the values on each face, and per region the inverse
+        transpose of the rows (v[J[j,k]], -1), k <= ndim (epigraph.py:84-100)."""
+        if self._pieces is None:
+            d = self.data
+            if self.If is None:
+                raise ValueError("EpigraphSupp needs the faces If")
+            n1 = d.ndim + 1
+            rows, off = [], [0]
+            for j in range(d.nregions):
+                pts = d.v[d.J[j]]
+                for i in range(d.nfuns):
+                    faces = np.asarray(self.If[i][j], dtype=np.int64).reshape(-1, n1)
+                    P = pts[faces]                                 # (nf, n1, ndim)
+                    vals = d.b[i, d.J[j]][faces]                   # (nf, n1)
+                    M = P[:, 1:] - P[:, :1]
+                    c = np.linalg.solve(M, (vals[:, 1:] - vals[:, :1])[..., None])[..., 0]
+                    eq = np.empty((faces.shape[0], n1))
+                    eq[:, :-1] = c
+                    eq[:, -1] = vals[:, 0] - (c * P[:, 0]).sum(axis=-1)
+                    rows.append(eq)
+                    off.append(off[-1] + eq.shape[0])
+            chk = -np.ones((d.nregions, n1, n1))
+            chk[:, :, :-1] = d.v[d.J[:, :n1]]
+            chk = np.linalg.inv(chk).transpose(0, 2, 1)
+            self._pieces = (np.asarray(off, np.int64), np.concatenate(rows, axis=0),
+                            np.ascontiguousarray(chk))
+        return self._pieces
+
+    def _eval_gpu(self, x):
+        from opymize_gb300.gpuarray import DeviceArray
+        if self._supp_dev is None:
+            off, eqns, chk = self.pieces()
+            self._supp_dev = (DeviceArray.to_gpu(off), DeviceArray.to_gpu(eqns),
+                              DeviceArray.to_gpu(chk))
+        return _epigraph_eval(self.data, 1, x, self._supp_dev)
+
+
+EpigraphSupportFct = EpigraphSupp

@@ -124,3 +124,105 @@ class QuadEpiProj(Operator):
         y = _inplace(x, y)
         _lib.call("opyx_quadepiproj", y.dcode, self.N, self.M, self.alph, self._sptr(y.dtype),
                   self.lbd, y.ptr, stream_ptr())
+
+
+def epigraph_Ab(I, J, v, b):
+    """The constraint system of EpigraphProj as one block-diagonal CSR matrix
+    and right-hand side (opymize/operators/proj.py:376-386): instance (j, i)
+    contributes the rows (v[l], -1) <= b[i, l] for l in J[j] with I[i, l]."""
+    import scipy.sparse as sp
+    nfuns, npoints = I.shape
+    blocks, rhs = [], []
+    for j in range(J.shape[0]):
+        for i in range(nfuns):
+            ls = [int(l) for l in J[j] if I[i, l]]
+            A = -np.ones((len(ls), v.shape[1] + 1))
+            A[:, :-1] = v[ls]
+            blocks.append(A)
+            rhs.append(np.asarray(b[i, ls], dtype=np.float64))
+    return sp.block_diag(blocks, format="csr"), np.concatenate(rhs)
+
+
+class _EpigraphData(object):
+    """Device copies of (I, J, v, b) and the opyx_epigraph descriptor."""
+
+    def __init__(self, I, J, v, b):
+        I, J = np.asarray(I), np.asarray(J)
+        v, b = np.asarray(v, dtype=np.float64), np.asarray(b, dtype=np.float64)
+        assert I.shape == b.shape and I.shape[1] == v.shape[0]
+        assert J.ndim == 2 and v.ndim == 2
+        if J.size and (J.min() < 0 or J.max() >= I.shape[1]):
+            raise ValueError("J holds indices outside [0, npoints)")
+        if not 1 <= v.shape[1] <= 3:
+            raise NotImplementedError("epigraph projections support ndim 1..3")
+        self.I, self.J, self.v, self.b = I, J, v, b
+        self.nfuns, self.npoints = I.shape
+        self.nregions, self.nsubpoints = J.shape
+        self.ndim = v.shape[1]
+        self._dev = {}
+        self._ij = None
+
+    def struct(self, dtype, supp=None):
+        if self._ij is None:
+            self._ij = (DeviceArray.to_gpu(np.ascontiguousarray(self.I, dtype=np.uint8)),
+                        DeviceArray.to_gpu(np.ascontiguousarray(self.J, dtype=np.int64)))
+        key = np.dtype(dtype).str
+        if key not in self._dev:
+            self._dev[key] = (DeviceArray.to_gpu(np.ascontiguousarray(self.v), dtype),
+                              DeviceArray.to_gpu(np.ascontiguousarray(self.b), dtype))
+        e = _lib.opyx_epigraph()
+        e.ndim, e.nsubpoints = self.ndim, self.nsubpoints
+        e.nfuns, e.nregions, e.npoints = self.nfuns, self.nregions, self.npoints
+        e.I, e.J = self._ij[0].ptr, self._ij[1].ptr
+        e.v, e.b = self._dev[key][0].ptr, self._dev[key][1].ptr
+        if supp is not None:
+            e.eq_off, e.eqns, e.checks = (a.ptr for a in supp)
+        return e
+
+
+class EpigraphProj(Operator):
+    """T(x)[j,i] = projection of x[j,i] onto the epigraph of the conjugate
+    of the convex piece j of the piecewise-linear function i, i.e. onto
+    {y : <v[k], y[:-1]> - y[-1] <= b[i,k] for k in J[j] with I[i,k]}
+    (opymize/operators/proj.py:388-480).
+
+    Every instance is solved by one thread with an active-set QP (the
+    reference's GPU method, proj.cu:660-790); the iteration bound and the
+    tolerance are the reference's (ndim*nsubpoints, 1e-9).  Instances that
+    hit the bound keep their last iterate and are counted in
+    ``nonconverged`` (the reference prints a warning)."""
+
+    def __init__(self, I, J, v, b, Ab=None):
+        Operator.__init__(self)
+        self.data = _EpigraphData(I, J, v, b)
+        d = self.data
+        self.I, self.J, self.v, self.b = d.I, d.J, d.v, d.b
+        self._Ab = Ab
+        self.x = Variable((d.nregions, d.nfuns, d.ndim + 1))
+        self.y = self.x
+        self.maxiter = d.ndim * d.nsubpoints
+        self.tol = 1e-9
+        self._count = None
+
+    @property
+    def Ab(self):
+        if self._Ab is None:
+            self._Ab = epigraph_Ab(self.I, self.J, self.v, self.b)
+        return self._Ab
+
+    @property
+    def nonconverged(self):
+        """Instances that hit the iteration bound, over all calls so far."""
+        return 0 if self._count is None else int(self._count.t.item())
+
+    def _call_gpu(self, x, y=None, add=False, jacobian=False):
+        assert not add
+        assert not jacobian
+        assert x.size == self.x.size, "x must hold (nregions, nfuns, ndim+1) values"
+        out = x if y is None else y
+        assert out.size == x.size and out.dtype == x.dtype
+        if self._count is None:
+            from opymize_gb300.gpuarray import torch
+            self._count = DeviceArray(torch().zeros(1, dtype=torch().int32, device="cuda"))
+        _lib.call("opyx_epigraph_proj", self.data.struct(x.dtype), x.dcode, x.ptr, out.ptr,
+                  int(self.maxiter), float(self.tol), self._count.ptr, stream_ptr())

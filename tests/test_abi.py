@@ -56,6 +56,7 @@ STRUCTS = {
     "opyx_step": _lib.opyx_step,
     "opyx_adaptive_state": _lib.opyx_adaptive_state,
     "opyx_fct": _lib.opyx_fct,
+    "opyx_epigraph": _lib.opyx_epigraph,
     "opyx_rof_problem": _lib.opyx_rof_problem,
     "opyx_rof_buffers": _lib.opyx_rof_buffers,
     "opyx_rof_info": _lib.opyx_rof_info,
