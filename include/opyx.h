@@ -179,7 +179,10 @@ int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y
                        int maxiter, double tol, unsigned* nonconv, void* stream);
 /* out (device double[2]) = {val, infeas} of EpigraphInd (which = 0,
  * epigraph.py:40-46) or EpigraphSupp (which = 1, epigraph.py:101-112) at x,
- * reduced in FP64; ws as for opyx_fct_eval. */
+ * reduced in FP64; ws as for opyx_fct_eval.  EpigraphSupp takes the max over
+ * the given faces (eq_off, eqns); with eq_off = NULL (ndim 1 only) it
+ * evaluates the convex envelope of each instance's points directly, which
+ * equals the faces' max when the faces are the points' lower convex hull. */
 int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void* x,
                        double* out, void* ws, void* stream);
 

@@ -261,15 +261,51 @@ k_eval(opyx_epigraph e, int which, const T* __restrict__ x, double* out, double*
         inf = fmax(inf, -s);
       }
       const double xt = fmax(2.220446049250313e-16, fabs(xi[ND]));
-      double best = -INFINITY;
-      for (int64_t f = e.eq_off[t]; f < e.eq_off[t + 1]; ++f) {
-        const double* eq = e.eqns + f * N1;
-        double s = eq[ND];
+      if (e.eq_off) {
+        double best = -INFINITY;
+        for (int64_t f = e.eq_off[t]; f < e.eq_off[t + 1]; ++f) {
+          const double* eq = e.eqns + f * N1;
+          double s = eq[ND];
 #pragma unroll
-        for (int q = 0; q < ND; ++q) s += eq[q] * (xi[q] / xt);
-        best = fmax(best, s);
+          for (int q = 0; q < ND; ++q) s += eq[q] * (xi[q] / xt);
+          best = fmax(best, s);
+        }
+        if (e.eq_off[t + 1] > e.eq_off[t]) val += xt * best;
+      } else if (ND == 1) {
+        // no faces given (1-D only): the convex envelope of the points
+        // (v_l, b_il), l in J[j], at p = x[0]/xt, as the smallest chord
+        // value over the point pairs bracketing p (p is clamped to the
+        // points' range; the region check above flags points outside)
+        const T* v = (const T*)e.v;
+        const T* b = (const T*)e.b;
+        const int64_t* jr = e.J + j * e.nsubpoints;
+        const uint8_t* ir = e.I + i * e.npoints;
+        double lo = INFINITY, hi = -INFINITY;
+        for (int k = 0; k < e.nsubpoints; ++k) {
+          if (!ir[jr[k]]) continue;
+          const double vk = (double)v[jr[k]];
+          lo = fmin(lo, vk);
+          hi = fmax(hi, vk);
+        }
+        const double p = fmin(hi, fmax(lo, xi[0] / xt));
+        double best = INFINITY;
+        for (int a = 0; a < e.nsubpoints; ++a) {
+          const int64_t la = jr[a];
+          if (!ir[la]) continue;
+          const double va = (double)v[la], ba = (double)b[i * e.npoints + la];
+          if (va == p) { best = fmin(best, ba); continue; }
+          if (va > p) continue;
+          for (int c = 0; c < e.nsubpoints; ++c) {
+            const int64_t lc = jr[c];
+            if (!ir[lc]) continue;
+            const double vc = (double)v[lc];
+            if (!(vc > p)) continue;
+            const double bc = (double)b[i * e.npoints + lc];
+            best = fmin(best, (ba * (vc - p) + bc * (p - va)) / (vc - va));
+          }
+        }
+        if (best < INFINITY) val += xt * best;
       }
-      if (e.eq_off[t + 1] > e.eq_off[t]) val += xt * best;
     }
   }
   double vals[2] = {val, inf};
@@ -327,7 +363,9 @@ int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void*
   int st = check(e);
   if (st) return st;
   if (which != 0 && which != 1) return OPYX_ERR_ARG;
-  if (which == 1 && (!e->eq_off || !e->eqns || !e->checks)) return OPYX_ERR_ARG;
+  if (which == 1 && !e->checks) return OPYX_ERR_ARG;
+  if (which == 1 && !e->eq_off && e->ndim != 1) return OPYX_ERR_UNSUPPORTED;
+  if (which == 1 && e->eq_off && !e->eqns) return OPYX_ERR_ARG;
   if (!out || !ws || ((uintptr_t)ws & 7)) return OPYX_ERR_WORKSPACE;
   const int64_t total = e->nregions * e->nfuns;
   if (total > 0 && !x) return OPYX_ERR_ARG;

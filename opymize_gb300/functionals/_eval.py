@@ -28,5 +28,8 @@ def devcopy(owner, name, host, dtype):
     cache = owner.__dict__.setdefault("_devcache", {})
     key = (name, np.dtype(dtype).str)
     if key not in cache:
-        cache[key] = DeviceArray.to_gpu(np.ascontiguousarray(host, dtype=dtype))
+        # float data is uploaded in its host precision and converted on the
+        # device (a host-side cast of a 2048^2 x 3 image costs more than
+        # the whole solve)
+        cache[key] = DeviceArray.to_gpu(host, dtype)
     return cache[key]

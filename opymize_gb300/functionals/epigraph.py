@@ -172,10 +172,18 @@ class EpigraphSupp(Functional):
         self._supp_dev = None
         self.conj = EpigraphInd(I, If, J, v, b, conj=self) if conj is None else conj
 
+    def checks(self):
+        """Per region the inverse transpose of the rows (v[J[j,k]], -1),
+        k <= ndim: the region's simplex test (epigraph.py:98-100)."""
+        d = self.data
+        n1 = d.ndim + 1
+        chk = -np.ones((d.nregions, n1, n1))
+        chk[:, :, :-1] = d.v[d.J[:, :n1]]
+        return np.ascontiguousarray(np.linalg.inv(chk).transpose(0, 2, 1))
+
     def pieces(self):
-        """(eq_off, eqns, checks): per instance (j, i) the affine functions
-        c.p + d through the values on each face, and per region the inverse
-        transpose of the rows (v[J[j,k]], -1), k <= ndim (epigraph.py:84-100)."""
+        """(eq_off, eqns): per instance (j, i) the affine functions c.p + d
+        through the values on each face If[i][j] (epigraph.py:84-97)."""
         if self._pieces is None:
             d = self.data
             if self.If is None:
@@ -195,19 +203,24 @@ class EpigraphSupp(Functional):
                     eq[:, -1] = vals[:, 0] - (c * P[:, 0]).sum(axis=-1)
                     rows.append(eq)
                     off.append(off[-1] + eq.shape[0])
-            chk = -np.ones((d.nregions, n1, n1))
-            chk[:, :, :-1] = d.v[d.J[:, :n1]]
-            chk = np.linalg.inv(chk).transpose(0, 2, 1)
-            self._pieces = (np.asarray(off, np.int64), np.concatenate(rows, axis=0),
-                            np.ascontiguousarray(chk))
+            self._pieces = (np.asarray(off, np.int64), np.concatenate(rows, axis=0))
         return self._pieces
 
     def _eval_gpu(self, x):
+        """Faces given: max over their affine functions, as the reference.
+        If = None (ndim 1): the convex envelope of each instance's points,
+        evaluated on the device (the same value when the faces are the lower
+        convex hull, without a host loop over every instance)."""
         from opymize_gb300.gpuarray import DeviceArray
         if self._supp_dev is None:
-            off, eqns, chk = self.pieces()
-            self._supp_dev = (DeviceArray.to_gpu(off), DeviceArray.to_gpu(eqns),
-                              DeviceArray.to_gpu(chk))
+            chk = DeviceArray.to_gpu(self.checks())
+            if self.If is None:
+                if self.data.ndim != 1:
+                    raise ValueError("EpigraphSupp without faces needs ndim 1")
+                self._supp_dev = (None, None, chk)
+            else:
+                off, eqns = self.pieces()
+                self._supp_dev = (DeviceArray.to_gpu(off), DeviceArray.to_gpu(eqns), chk)
         return _epigraph_eval(self.data, 1, x, self._supp_dev)
 
 

@@ -12,7 +12,7 @@ def _dev_cache(owner, name, host, dtype):
     cache = owner.__dict__.setdefault("_devcache", {})
     key = (name, np.dtype(dtype).str)
     if key not in cache:
-        cache[key] = DeviceArray.to_gpu(np.ascontiguousarray(host, dtype=dtype))
+        cache[key] = DeviceArray.to_gpu(host, dtype)   # float casts run on the device
     return cache[key]
 
 

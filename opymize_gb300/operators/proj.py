@@ -176,7 +176,7 @@ class _EpigraphData(object):
         e.I, e.J = self._ij[0].ptr, self._ij[1].ptr
         e.v, e.b = self._dev[key][0].ptr, self._dev[key][1].ptr
         if supp is not None:
-            e.eq_off, e.eqns, e.checks = (a.ptr for a in supp)
+            e.eq_off, e.eqns, e.checks = (None if a is None else a.ptr for a in supp)
         return e
 
 

@@ -155,3 +155,43 @@ def epigraph_supp(eq_off, eqns, checks, x):
             t = j * nfuns + i
             val += xt * float((eqns[eq_off[t]:eq_off[t + 1]] @ xh).max())
     return val, inf
+
+
+def region_checks(J, v):
+    """checks[j] = inverse transpose of the rows (v[J[j,k]], -1), k <= ndim."""
+    ndim = v.shape[1]
+    chk = -np.ones((J.shape[0], ndim + 1, ndim + 1))
+    chk[:, :, :-1] = v[J[:, :ndim + 1]]
+    return np.linalg.inv(chk).transpose(0, 2, 1)
+
+
+def epigraph_supp_envelope(I, J, v, b, x):
+    """EpigraphSupp value for ndim 1 without faces: xt * conv(points)(p) at
+    p = x[0]/xt (clamped to the points' range), the convex envelope taken as
+    the smallest chord over point pairs bracketing p."""
+    assert v.shape[1] == 1
+    chk = region_checks(J, v)
+    nregions, nfuns, _ = x.shape
+    val, inf = 0.0, 0.0
+    for j in range(nregions):
+        for i in range(nfuns):
+            xi = x[j, i].astype(np.float64)
+            inf = max(inf, float(np.max(np.fmax(0.0, -(chk[j] @ xi)))))
+            xt = max(np.spacing(1), abs(xi[-1]))
+            ls = [int(l) for l in J[j] if I[i, l]]
+            vs, bs = v[ls, 0], b[i, ls]
+            p = min(vs.max(), max(vs.min(), xi[0] / xt))
+            best = np.inf
+            for a in range(len(ls)):
+                if vs[a] == p:
+                    best = min(best, bs[a])
+                    continue
+                if vs[a] > p:
+                    continue
+                for c in range(len(ls)):
+                    if vs[c] > p:
+                        best = min(best, (bs[a] * (vs[c] - p) + bs[c] * (p - vs[a]))
+                                   / (vs[c] - vs[a]))
+            if best < np.inf:
+                val += xt * best
+    return val, inf

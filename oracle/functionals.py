@@ -394,3 +394,46 @@ class MaskedAffineFct(Functional):
         def op(x):
             x[:] = scale * (x + (-tau) * c)
         return op
+
+
+class EpigraphInd(Functional):
+    """0 if every instance lies in its epigraph, else inf
+    (opymize/functionals/epigraph.py:7-54); prox = EpigraphProj."""
+
+    def __init__(self, I, If, J, v, b, conj=None):
+        from oracle import epigraph as E
+        self.E = E
+        self.I, self.If, self.J, self.v, self.b = np.asarray(I, bool), If, J, v, b
+        self.shape = (J.shape[0], I.shape[0], v.shape[1] + 1)
+        self.size = int(np.prod(self.shape))
+        self.conj = EpigraphSupp(I, If, J, v, b, conj=self) if conj is None else conj
+
+    def __call__(self, x):
+        return self.E.epigraph_ind(self.I, self.J, self.v, self.b, x.reshape(self.shape))
+
+    def prox(self, tau):
+        def op(x):
+            y, _ = self.E.epigraph_proj(self.I, self.J, self.v, self.b, x.reshape(self.shape))
+            x[:] = y.ravel()
+        return op
+
+
+class EpigraphSupp(Functional):
+    """Support function of the epigraphs (opymize/functionals/epigraph.py:56-112);
+    with If = None (ndim 1) its value is the convex envelope of each
+    instance's points, computed directly."""
+
+    def __init__(self, I, If, J, v, b, conj=None):
+        from oracle import epigraph as E
+        self.E = E
+        self.I, self.If, self.J, self.v, self.b = np.asarray(I, bool), If, J, v, b
+        self.shape = (J.shape[0], I.shape[0], v.shape[1] + 1)
+        self.size = int(np.prod(self.shape))
+        self.conj = EpigraphInd(I, If, J, v, b, conj=self) if conj is None else conj
+
+    def __call__(self, x):
+        x = x.reshape(self.shape)
+        if self.If is not None:
+            off, eqns, chk = self.E.supp_pieces(self.I, self.If, self.J, self.v, self.b)
+            return self.E.epigraph_supp(off, eqns, chk, x)
+        return self.E.epigraph_supp_envelope(self.I, self.J, self.v, self.b, x)

@@ -91,11 +91,11 @@ def ref_ind(I, J, v, b):
     return EpigraphInd(I, None, J, v, b, conj=conj)
 
 
-def ref_supp(I, If, J, v, b):
-    """The reference's EpigraphSupp.  Its face equations (epigraph.py:86-97)
-    pass a stack of right-hand-side vectors to np.linalg.solve, which numpy
-    >= 2 reads as a matrix; the numpy 1 meaning is restored for the
-    constructor only."""
+def ref_supp(I, If, J, v, b, with_conj=False):
+    """The reference's EpigraphSupp (with its conjugate EpigraphInd when
+    `with_conj`).  Its face equations (epigraph.py:86-97) pass a stack of
+    right-hand-side vectors to np.linalg.solve, which numpy >= 2 reads as a
+    matrix; the numpy 1 meaning is restored for the constructor only."""
     orig = np.linalg.solve
 
     def solve_stacked_vectors(a, rhs):
@@ -106,6 +106,8 @@ def ref_supp(I, If, J, v, b):
 
     np.linalg.solve = solve_stacked_vectors
     try:
+        if with_conj:
+            return EpigraphSupp(I, If, J, v, b)
         return EpigraphSupp(I, If, J, v, b, conj=types.SimpleNamespace())
     finally:
         np.linalg.solve = orig

@@ -1,0 +1,98 @@
+"""The sublabel lifting workload on the GPU's generic PDHG path (BlockOp /
+SplitSum of IdentityOp, IndexedMultAdj, MatrixMultR, ScaleOp, GradientOp,
+PositivityFct, IndicatorFct, L1Norms, EpigraphSupp) against the reference's
+own PDHG run of the same model (tests/golden/sublabel_*.npz).
+Bars: FP64 relative L2 <= 1e-10 of x and y after each dumped iteration;
+FP32 <= 1e-4 (the epigraph QP's active sets are decided at the 1e-9
+tolerance of the reference, which FP32 iterates cross differently)."""
+
+import numpy as np
+import pytest
+
+from tests.test_sublabel import CASES, load, fixture_faces
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_solver(z, faces=True):
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.tools import lifting
+    img = z["img"]
+    g, f, A, d = lifting.sublabel_problem(img, L=int(z["L"]), lbd=float(z["lbd"]),
+                                          samples=int(z["samples"]), trunc=float(z["trunc"]),
+                                          with_faces=False)
+    if faces:
+        supp = f.fcts[-1]
+        supp.If = fixture_faces(z, int(z["L"]), img.size)
+    return PDHG(g, f, A)
+
+
+def run(z, precision, faces=True):
+    s = gpu_solver(z, faces)
+    rec = {}
+
+    def cb(state, info):
+        rec[info["iter"]] = (state[0].copy(), state[1].copy(), dict(info))
+
+    np.random.seed(0)
+    s.solve(steps=str(z["steps"]), precision=precision, term_pd_gap=1e-300,
+            term_maxiter=int(z["iters"]), granularity=int(z["gran"]), cbfun=cb)
+    assert s.path == "generic"
+    return s, rec
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a, np.float64) - b) / max(1e-300, np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_matches_reference(name):
+    z = load(name)
+    s, rec = run(z, "double")
+    for k, it in enumerate(z["dump_iters"]):
+        x, y, info = rec[int(it)]
+        assert rel(x, z["x"][k]) <= 1e-10, (name, it, rel(x, z["x"][k]))
+        assert rel(y, z["y"][k]) <= 1e-10, (name, it, rel(y, z["y"][k]))
+        ref = z["info"][k]
+        assert info["objp"] == pytest.approx(ref[1], rel=1e-9, abs=1e-9)
+        assert info["objd"] == pytest.approx(ref[2], rel=1e-9, abs=1e-9)
+        assert info["infeasp"] == pytest.approx(ref[4], rel=1e-6, abs=1e-9)
+        assert info["infeasd"] == pytest.approx(ref[5], rel=1e-6, abs=1e-9)
+    assert s.f.fcts[-1].conj.prox(1.0).nonconverged == 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_matches_reference(name):
+    z = load(name)
+    _, rec = run(z, "float")
+    k = len(z["dump_iters"]) - 1
+    x, y, _ = rec[int(z["dump_iters"][k])]
+    assert rel(x, z["x"][k]) <= 1e-4 and rel(y, z["y"][k]) <= 1e-4
+
+
+def test_envelope_gap_equals_faces_gap():
+    z = load(CASES[0])
+    _, ra = run(z, "double", faces=True)
+    _, rb = run(z, "double", faces=False)
+    for it in ra:
+        assert ra[it][2]["objp"] == pytest.approx(rb[it][2]["objp"], rel=1e-12, abs=1e-12)
+
+
+def test_full_size_iterates():
+    """512 x 512, 16 labels, FP32: the workload's shape runs, the QP always
+    converges, and the state stays finite and feasible in its cones."""
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.tools import lifting
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    img = np.clip(piecewise_constant((512, 512), 1, sigma=0.05, seed=1,
+                                     salt_pepper=0.1)[..., 0], 0, 1)
+    g, f, A, d = lifting.sublabel_problem(img, L=16, lbd=0.1, samples=8)
+    s = PDHG(g, f, A)
+    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=100,
+            granularity=50)
+    x, y = s.state
+    assert np.isfinite(x).all() and np.isfinite(y).all()
+    assert f.fcts[-1].conj.prox(1.0).nonconverged == 0
+    assert np.isfinite(s.info["objp"]) and np.isfinite(s.info["objd"])
+    u = x[:512 * 512 * 16].reshape(-1, 16)
+    assert u.min() >= 0
