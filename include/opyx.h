@@ -203,6 +203,12 @@ typedef struct {
 int opyx_shiftscale(int dtype, int64_t n, const void* a_vec, double a,
                     const void* b_vec, double b, const void* shift_vec, double shift,
                     const void* x, void* y, int add, void* stream);
+/* y = a*(x - tau*c), a and c a device vector or (NULL) the scalar given, tau
+ * an opyx_step: the prox of tau*AffineFct / MaskedAffineFct
+ * (opymize/functionals/affine.py:38-42, :86-90, which set ShiftScaleOp's b to
+ * -tau) for scalar, per-element and device-held adaptive steps alike. */
+int opyx_affine_prox(int dtype, int64_t n, const void* a_vec, double a, const void* c_vec,
+                     double c, opyx_step tau, const void* x, void* y, void* stream);
 /* SSD prox: y = (x + t*f)/(1 + t) with t = tau*vol_k on masked pixels, y = x
  * elsewhere; x, y, f (N,C); vol device double[C] (NULL = ones); mask device
  * uint8[N] (NULL = all).  SSD.prox -> ShiftScaleOp (functionals/quad.py:45-55). */

@@ -129,6 +129,7 @@ SIGNATURES = {
     "opyx_indexedmult": (i32, [i32, i32, i64, i32, i32, i32, vp, vp, vp, vp, i32, vp]),
     "opyx_indexedmult_adj": (i32, [i32, i32, i64, i32, i32, i32, vp, vp, vp, vp, i32, vp]),
     "opyx_shiftscale": (i32, [i32, i64, vp, f64, vp, f64, vp, f64, vp, vp, i32, vp]),
+    "opyx_affine_prox": (i32, [i32, i64, vp, f64, vp, f64, opyx_step, vp, vp, vp]),
     "opyx_ssd_prox": (i32, [i32, i64, i32, vp, vp, vp, opyx_step, vp, vp, vp]),
     "opyx_posproj": (i32, [i32, i64, vp, vp, i32, vp]),
     "opyx_negproj": (i32, [i32, i64, vp, vp, i32, vp]),

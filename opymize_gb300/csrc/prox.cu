@@ -24,6 +24,17 @@ __global__ void k_shiftscale(int64_t n, const T* __restrict__ av, T a, const T* 
   }
 }
 
+// y = a*(x - tau*c): prox of tau*(b + <c, x>) (masked by a)
+template <typename T>
+__global__ void k_affine_prox(int64_t n, const T* __restrict__ av, T a, const T* __restrict__ cv,
+                              T c, StepT<T> tau, const T* __restrict__ x, T* __restrict__ y) {
+  GRID_STRIDE(i, n) {
+    const T ai = av ? av[i] : a;
+    const T ci = cv ? cv[i] : c;
+    y[i] = ai * (x[i] - tau.at(i) * ci);
+  }
+}
+
 template <typename T>
 __global__ void k_ssd_prox(int64_t N, int C, const T* __restrict__ f, const double* __restrict__ vol,
                            const uint8_t* __restrict__ mask, StepT<T> tau,
@@ -108,6 +119,13 @@ int opyx_shiftscale(int dtype, int64_t n, const void* a_vec, double a, const voi
   if (n < 0 || (n > 0 && (!x || !y))) return OPYX_ERR_ARG;
   LAUNCH(k_shiftscale, n, n, (const T*)a_vec, (T)a, (const T*)b_vec, (T)b,
          (const T*)shift_vec, (T)shift, (const T*)x, (T*)y, add);
+}
+
+int opyx_affine_prox(int dtype, int64_t n, const void* a_vec, double a, const void* c_vec,
+                     double c, opyx_step tau, const void* x, void* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return OPYX_ERR_ARG;
+  LAUNCH(k_affine_prox, n, n, (const T*)a_vec, (T)a, (const T*)c_vec, (T)c, StepT<T>(tau),
+         (const T*)x, (T*)y);
 }
 
 int opyx_ssd_prox(int dtype, int64_t N, int C, const void* f, const double* vol,

@@ -5,7 +5,8 @@ import numpy as np
 
 from opymize_gb300 import Variable, Functional
 from opymize_gb300.functionals._eval import fct, evaluate, devcopy
-from opymize_gb300.operators import ConstOp, ConstrainOp, PosProj, NegProj, ShiftScaleOp
+from opymize_gb300.operators import ConstOp, ConstrainOp, PosProj, NegProj
+from opymize_gb300.operators.affine import AffineProxOp
 
 
 class AffineFct(Functional):
@@ -16,7 +17,6 @@ class AffineFct(Functional):
         self.b, self.c = b, c
         self.x = Variable(N)
         self.conj = IndicatorFct(N, c1=c, c2=b, conj=self) if conj is None else conj
-        self._prox = ShiftScaleOp(N, self.c, 1, -1)
 
     def _eval_gpu(self, x):
         kw = dict(scalar0=float(self.b))
@@ -27,8 +27,8 @@ class AffineFct(Functional):
         return evaluate(fct("affine", self.x.size, 1, **kw), x)
 
     def prox(self, tau):
-        self._prox.b = -tau
-        return self._prox
+        """x - tau*c (affine.py:38-42) for any kind of step."""
+        return AffineProxOp(self.x.size, 1.0, self.c, tau)
 
 
 class ConstFct(AffineFct):
@@ -61,7 +61,7 @@ class MaskedAffineFct(Functional):
         self.conj = ConstrainFct(mask, c, conj=self) if conj is None else conj
         scale = np.zeros(c.shape)
         scale[self.mask, :] = 1.0
-        self._prox = ShiftScaleOp(self.x.size, self.c.ravel(), scale.ravel(), -1)
+        self._scale = scale.ravel()
 
     def _eval_gpu(self, x):
         N, M = self.c.shape
@@ -69,8 +69,8 @@ class MaskedAffineFct(Functional):
                             mask=devcopy(self, "m", self.mask.astype(np.uint8), np.uint8).ptr), x)
 
     def prox(self, tau):
-        self._prox.b = -tau
-        return self._prox
+        """mask*(x - tau*c) (affine.py:86-90) for any kind of step."""
+        return AffineProxOp(self.x.size, self._scale, self.c.ravel(), tau)
 
 
 class IndicatorFct(Functional):

@@ -90,6 +90,35 @@ class ShiftScaleOp(Operator):
             return ScaleOp(self.x.size, self.a)
 
 
+class AffineProxOp(Operator):
+    """T(x) = a*(x - tau*c): the prox of tau*(b + <c, x>), masked by a
+    (AffineFct / MaskedAffineFct.prox, opymize/functionals/affine.py:38-42,
+    :86-90).  ``tau`` is a scalar, a per-element DeviceArray or a
+    DeviceScalar (adaptive steps), read by the kernel at launch."""
+
+    def __init__(self, N, a, c, tau):
+        Operator.__init__(self)
+        self.a, self.c, self.tau = a, c, tau
+        self.x = Variable(N)
+        self.y = Variable(N)
+
+    def _arg(self, name, v, dtype):
+        if isinstance(v, np.ndarray) and v.size > 1:
+            return _dev_cache(self, name, v.ravel(), dtype).ptr, 0.0
+        return None, float(np.asarray(v).ravel()[0]) if isinstance(v, np.ndarray) else float(v)
+
+    def _call_gpu(self, x, y=None, add=False, jacobian=False):
+        assert not add
+        y = x if y is None else y
+        ap, av = self._arg("a", self.a, x.dtype)
+        cp, cv = self._arg("c", self.c, x.dtype)
+        _lib.call("opyx_affine_prox", x.dcode, x.size, ap, av, cp, cv,
+                  step_struct(self.tau, x.dtype), x.ptr, y.ptr, stream_ptr())
+        if jacobian:
+            from opymize_gb300.linear.scale import ScaleOp
+            return ScaleOp(self.x.size, self.a)
+
+
 class SSDProxOp(Operator):
     """prox of tau*SSD: x <- (x + t*f)/(1 + t), t = tau*vol on masked pixels
     (opymize/functionals/quad.py:45-55 builds the same map as a ShiftScaleOp
