@@ -17,7 +17,8 @@ from tests.test_oracle import build_problem
 pytestmark = pytest.mark.gpu
 
 SOLVER_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN)
-                      if f.endswith(".npz") and f not in ("ops.npz", "epigraph.npz"))
+                      if f.endswith(".npz") and f not in ("ops.npz", "epigraph.npz")
+                      and not f.startswith("sublabel"))
 SMALL_CASES = [c for c in SOLVER_CASES if c != "rof_gray256_adaptive"]
 
 
