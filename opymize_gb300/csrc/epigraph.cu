@@ -11,8 +11,8 @@
 // is solved per thread with the primal active-set method (Nocedal & Wright,
 // Numerical Optimization, 2nd ed., Algorithm 16.3), as the reference does.
 // The equality-constrained subproblems and the Lagrange multipliers come from
-// the Gram matrix G = A_W A_W^T of the working set W (|W| <= n+1 <= 4), solved
-// by Gaussian elimination with partial pivoting, for every n alike.
+// an orthonormal basis of the working set's normals (|W| <= n+1 <= 4), for
+// every n alike (ActiveBasis below).
 #include "common.cuh"
 
 namespace opyx {
@@ -39,72 +39,106 @@ OPYX_D T adot(const T* vl, const T* y) {
   return s;
 }
 
-// <a_l, a_m> = <v_l, v_m> + 1
+// Orthonormal basis q_0..q_{m-1} of span{a_w : w in W}, built by modified
+// Gram-Schmidt (two passes) from e_0 = a_{W0} and the differences
+// e_i = a_{Wi} - a_{W0} = (v_{Wi} - v_{W0}, 0).  Neighbouring constraints
+// have nearly parallel normals; their difference vectors keep the basis well
+// conditioned where the Gram matrix A_W A_W^T would square the condition
+// number (which FP32 iterates cannot afford).  e_i = sum_{k<=i} R[k][i] q_k.
 template <typename T, int ND>
-OPYX_D T agram(const T* vl, const T* vm) {
-  T s = T(1);
-#pragma unroll
-  for (int k = 0; k < ND; ++k) s += vl[k] * vm[k];
-  return s;
-}
+struct ActiveBasis {
+  static constexpr int N1 = ND + 1;
+  T q[N1][N1];
+  T R[N1][N1];
+  int m;
 
-// Solve G z = r in place (r <- z) for the leading m x m block, m <= NA.
-// Returns false if a pivot is not above `tiny` times the largest diagonal.
-template <typename T, int NA>
-OPYX_D bool gauss_solve(T (&G)[NA][NA], T (&r)[NA], int m) {
-  T scale = T(0);
+  OPYX_D bool build(const T (&aw)[N1][ND], int m_) {
+    m = m_;
+    const T tiny = sizeof(T) == 4 ? T(1e-5) : T(1e-12);
 #pragma unroll
-  for (int a = 0; a < NA; ++a)
-    if (a < m) scale = fmax(scale, fabs(G[a][a]));
-  const T tiny = (sizeof(T) == 4 ? T(1e-6) : T(1e-13)) * scale;
+    for (int i = 0; i < N1; ++i) {
+      if (i >= m) break;
+      T e[N1];
 #pragma unroll
-  for (int c = 0; c < NA; ++c) {
-    if (c >= m) break;
-    int piv = c;
+      for (int k = 0; k < ND; ++k) e[k] = i == 0 ? aw[0][k] : aw[i][k] - aw[0][k];
+      e[ND] = i == 0 ? T(-1) : T(0);
+      T en = T(0);
 #pragma unroll
-    for (int a = c + 1; a < NA; ++a)
-      if (a < m && fabs(G[a][c]) > fabs(G[piv][c])) piv = a;
-    if (!(fabs(G[piv][c]) > tiny)) return false;
-    if (piv != c) {
+      for (int k = 0; k < N1; ++k) en += e[k] * e[k];
+      en = sqrt(en);
 #pragma unroll
-      for (int q = 0; q < NA; ++q) { T t = G[c][q]; G[c][q] = G[piv][q]; G[piv][q] = t; }
-      T t = r[c]; r[c] = r[piv]; r[piv] = t;
+      for (int c = 0; c < N1; ++c) R[c][i] = T(0);
+#pragma unroll
+      for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+        for (int c = 0; c < N1; ++c) {
+          if (c >= i) break;
+          T dot = T(0);
+#pragma unroll
+          for (int k = 0; k < N1; ++k) dot += q[c][k] * e[k];
+          R[c][i] += dot;
+#pragma unroll
+          for (int k = 0; k < N1; ++k) e[k] -= dot * q[c][k];
+        }
+      }
+      T nn = T(0);
+#pragma unroll
+      for (int k = 0; k < N1; ++k) nn += e[k] * e[k];
+      nn = sqrt(nn);
+      if (!(nn > tiny * en)) return false;   // dependent constraint
+      R[i][i] = nn;
+      const T inv = T(1) / nn;
+#pragma unroll
+      for (int k = 0; k < N1; ++k) q[i][k] = e[k] * inv;
     }
-    const T inv = T(1) / G[c][c];
-#pragma unroll
-    for (int a = c + 1; a < NA; ++a) {
-      if (a >= m) break;
-      const T f = G[a][c] * inv;
-#pragma unroll
-      for (int q = c; q < NA; ++q) G[a][q] -= f * G[c][q];
-      r[a] -= f * r[c];
-    }
+    return true;
   }
-#pragma unroll
-  for (int c = NA - 1; c >= 0; --c) {
-    if (c >= m) continue;
-    T s = r[c];
-#pragma unroll
-    for (int q = c + 1; q < NA; ++q)
-      if (q < m) s -= G[c][q] * r[q];
-    r[c] = s / G[c][c];
-  }
-  return true;
-}
 
-// Coefficients z of the least-squares fit A_W^T z ~ d (G z = A_W d).
-template <typename T, int ND>
-OPYX_D bool working_coeffs(const T (&aw)[ND + 1][ND], int m, const T* d, T (&z)[ND + 1]) {
-  constexpr int NA = ND + 1;
-  T G[NA][NA];
+  // p = d - Q Q^T d: the part of d orthogonal to the active normals
+  OPYX_D void project_out(const T* d, T* p) const {
 #pragma unroll
-  for (int a = 0; a < NA; ++a) {
-    z[a] = a < m ? adot<T, ND>(aw[a], d) : T(0);
+    for (int k = 0; k < N1; ++k) p[k] = d[k];
 #pragma unroll
-    for (int c = 0; c < NA; ++c) G[a][c] = (a < m && c < m) ? agram<T, ND>(aw[a], aw[c]) : T(0);
+    for (int c = 0; c < N1; ++c) {
+      if (c >= m) break;
+      T dot = T(0);
+#pragma unroll
+      for (int k = 0; k < N1; ++k) dot += q[c][k] * p[k];
+#pragma unroll
+      for (int k = 0; k < N1; ++k) p[k] -= dot * q[c][k];
+    }
   }
-  return gauss_solve<T, NA>(G, z, m);
-}
+
+  // lambda with A_W^T lambda = r in the least-squares sense: R mu = Q^T r,
+  // then lambda_i = mu_i (i >= 1), lambda_0 = mu_0 - sum_{i>=1} mu_i,
+  // since A_W^T lambda = (sum_i lambda_i) e_0 + sum_{i>=1} lambda_i e_i.
+  OPYX_D void multipliers(const T* r, T (&lam)[N1]) const {
+    T mu[N1];
+#pragma unroll
+    for (int c = 0; c < N1; ++c) {
+      T dot = T(0);
+#pragma unroll
+      for (int k = 0; k < N1; ++k) dot += q[c][k] * r[k];
+      mu[c] = c < m ? dot : T(0);
+    }
+#pragma unroll
+    for (int c = N1 - 1; c >= 0; --c) {
+      if (c >= m) continue;
+      T sum = mu[c];
+#pragma unroll
+      for (int k = c + 1; k < N1; ++k)
+        if (k < m) sum -= R[c][k] * mu[k];
+      mu[c] = sum / R[c][c];
+    }
+    T rest = T(0);
+#pragma unroll
+    for (int c = 1; c < N1; ++c) {
+      lam[c] = c < m ? mu[c] : T(0);
+      rest += lam[c];
+    }
+    lam[0] = mu[0] - rest;
+  }
+};
 
 // Projection of one instance.  Returns false when the method did not finish
 // within maxiter steps (the last iterate is kept, as the reference does).
@@ -135,16 +169,9 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     T d[N1], p[N1], z[NA];
 #pragma unroll
     for (int k = 0; k < N1; ++k) d[k] = x[k] - y[k];
-    if (!working_coeffs<T, ND>(aw, m, d, z)) return false;
-#pragma unroll
-    for (int k = 0; k < N1; ++k) p[k] = d[k];
-#pragma unroll
-    for (int a = 0; a < NA; ++a) {
-      if (a >= m) break;
-#pragma unroll
-      for (int k = 0; k < ND; ++k) p[k] -= z[a] * aw[a][k];
-      p[ND] += z[a];
-    }
+    ActiveBasis<T, ND> basis;
+    if (!basis.build(aw, m)) return false;
+    basis.project_out(d, p);
     T pn = T(0);
 #pragma unroll
     for (int k = 0; k < N1; ++k) pn += fabs(p[k]);
@@ -182,7 +209,8 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     // x - y = A_W^T lambda decide optimality
 #pragma unroll
     for (int k = 0; k < N1; ++k) d[k] = x[k] - y[k];
-    if (!working_coeffs<T, ND>(aw, m, d, z)) return false;
+    if (m > basis.m && !basis.build(aw, m)) return false;   // a constraint was added
+    basis.multipliers(d, z);
     int amin = -1;
     T lmin = T(0);
 #pragma unroll
@@ -272,36 +300,53 @@ k_eval(opyx_epigraph e, int which, const T* __restrict__ x, double* out, double*
         }
         if (e.eq_off[t + 1] > e.eq_off[t]) val += xt * best;
       } else if (ND == 1) {
-        // no faces given (1-D only): the convex envelope of the points
-        // (v_l, b_il), l in J[j], at p = x[0]/xt, as the smallest chord
-        // value over the point pairs bracketing p (p is clamped to the
-        // points' range; the region check above flags points outside)
+        // no faces given (1-D only): the convex envelope g of the points
+        // (v_l, b_il), l in J[j], at p = x[0]/xt -- the smallest chord over
+        // the point pairs bracketing p; outside the points' range the end
+        // edges of the lower hull are extended, which is what the max over
+        // the hull's faces gives there
         const T* v = (const T*)e.v;
         const T* b = (const T*)e.b;
         const int64_t* jr = e.J + j * e.nsubpoints;
         const uint8_t* ir = e.I + i * e.npoints;
-        double lo = INFINITY, hi = -INFINITY;
+        const T* bi = b + i * e.npoints;
+        double lo = INFINITY, hi = -INFINITY, blo = 0.0, bhi = 0.0;
         for (int k = 0; k < e.nsubpoints; ++k) {
           if (!ir[jr[k]]) continue;
-          const double vk = (double)v[jr[k]];
-          lo = fmin(lo, vk);
-          hi = fmax(hi, vk);
+          const double vk = (double)v[jr[k]], bk = (double)bi[jr[k]];
+          if (vk < lo || (vk == lo && bk < blo)) { lo = vk; blo = bk; }
+          if (vk > hi || (vk == hi && bk < bhi)) { hi = vk; bhi = bk; }
         }
-        const double p = fmin(hi, fmax(lo, xi[0] / xt));
+        const double p = xi[0] / xt;
         double best = INFINITY;
-        for (int a = 0; a < e.nsubpoints; ++a) {
-          const int64_t la = jr[a];
-          if (!ir[la]) continue;
-          const double va = (double)v[la], ba = (double)b[i * e.npoints + la];
-          if (va == p) { best = fmin(best, ba); continue; }
-          if (va > p) continue;
-          for (int c = 0; c < e.nsubpoints; ++c) {
-            const int64_t lc = jr[c];
-            if (!ir[lc]) continue;
-            const double vc = (double)v[lc];
-            if (!(vc > p)) continue;
-            const double bc = (double)b[i * e.npoints + lc];
-            best = fmin(best, (ba * (vc - p) + bc * (p - va)) / (vc - va));
+        if (lo == hi) {
+          best = blo;
+        } else if (p < lo || p > hi) {
+          // first edge: least chord slope out of the leftmost point; last
+          // edge: largest chord slope into the rightmost point
+          double s = p < lo ? INFINITY : -INFINITY;
+          for (int k = 0; k < e.nsubpoints; ++k) {
+            if (!ir[jr[k]]) continue;
+            const double vk = (double)v[jr[k]], bk = (double)bi[jr[k]];
+            if (p < lo && vk > lo) s = fmin(s, (bk - blo) / (vk - lo));
+            if (p > hi && vk < hi) s = fmax(s, (bhi - bk) / (hi - vk));
+          }
+          best = p < lo ? blo + s * (p - lo) : bhi + s * (p - hi);
+        } else {
+          for (int a = 0; a < e.nsubpoints; ++a) {
+            const int64_t la = jr[a];
+            if (!ir[la]) continue;
+            const double va = (double)v[la], ba = (double)bi[la];
+            if (va == p) { best = fmin(best, ba); continue; }
+            if (va > p) continue;
+            for (int c = 0; c < e.nsubpoints; ++c) {
+              const int64_t lc = jr[c];
+              if (!ir[lc]) continue;
+              const double vc = (double)v[lc];
+              if (!(vc > p)) continue;
+              const double bc = (double)bi[lc];
+              best = fmin(best, (ba * (vc - p) + bc * (p - va)) / (vc - va));
+            }
           }
         }
         if (best < INFINITY) val += xt * best;

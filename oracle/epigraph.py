@@ -166,9 +166,10 @@ def region_checks(J, v):
 
 
 def epigraph_supp_envelope(I, J, v, b, x):
-    """EpigraphSupp value for ndim 1 without faces: xt * conv(points)(p) at
-    p = x[0]/xt (clamped to the points' range), the convex envelope taken as
-    the smallest chord over point pairs bracketing p."""
+    """EpigraphSupp value for ndim 1 without faces: xt * g(p), p = x[0]/xt,
+    g the convex envelope of each instance's points (the smallest chord over
+    the pairs bracketing p; beyond the points' range the lower hull's end
+    edges extended, as the max over the hull's faces gives there)."""
     assert v.shape[1] == 1
     chk = region_checks(J, v)
     nregions, nfuns, _ = x.shape
@@ -179,19 +180,27 @@ def epigraph_supp_envelope(I, J, v, b, x):
             inf = max(inf, float(np.max(np.fmax(0.0, -(chk[j] @ xi)))))
             xt = max(np.spacing(1), abs(xi[-1]))
             ls = [int(l) for l in J[j] if I[i, l]]
-            vs, bs = v[ls, 0], b[i, ls]
-            p = min(vs.max(), max(vs.min(), xi[0] / xt))
-            best = np.inf
-            for a in range(len(ls)):
-                if vs[a] == p:
-                    best = min(best, bs[a])
-                    continue
-                if vs[a] > p:
-                    continue
-                for c in range(len(ls)):
-                    if vs[c] > p:
-                        best = min(best, (bs[a] * (vs[c] - p) + bs[c] * (p - vs[a]))
-                                   / (vs[c] - vs[a]))
-            if best < np.inf:
-                val += xt * best
+            vs, bs = v[ls, 0].astype(np.float64), b[i, ls].astype(np.float64)
+            lo, hi = vs.min(), vs.max()
+            blo, bhi = bs[vs == lo].min(), bs[vs == hi].min()
+            p = xi[0] / xt
+            if lo == hi:
+                best = blo
+            elif p < lo:
+                best = blo + min((bs[vs > lo] - blo) / (vs[vs > lo] - lo)) * (p - lo)
+            elif p > hi:
+                best = bhi + max((bhi - bs[vs < hi]) / (hi - vs[vs < hi])) * (p - hi)
+            else:
+                best = np.inf
+                for a in range(len(ls)):
+                    if vs[a] == p:
+                        best = min(best, bs[a])
+                        continue
+                    if vs[a] > p:
+                        continue
+                    for c in range(len(ls)):
+                        if vs[c] > p:
+                            best = min(best, (bs[a] * (vs[c] - p) + bs[c] * (p - vs[a]))
+                                       / (vs[c] - vs[a]))
+            val += xt * best
     return val, inf

@@ -107,3 +107,8 @@ def test_envelope_value_equals_faces_value():
         x[j, :, 0] = -x[j, :, 1] * (d["t"][j] + rng.random(x.shape[1]) * d["h"])
     a, b = supp(x.ravel()), nof(x.ravel())
     assert a[0] == pytest.approx(b[0], rel=1e-12) and a[1] == b[1] == 0
+    # also outside the regions (infeasible points): the hull's end edges
+    for _ in range(3):
+        x = rng.normal(0, 1, supp.shape)
+        a, b = supp(x.ravel()), nof(x.ravel())
+        assert a[0] == pytest.approx(b[0], rel=1e-12) and a[1] == pytest.approx(b[1])
