@@ -140,23 +140,47 @@ struct ActiveBasis {
   }
 };
 
-// Projection of one instance.  Returns false when the method did not finish
-// within maxiter steps (the last iterate is kept, as the reference does).
+// Largest violation max_l (a_l . y - b_l) over the instance's constraints
+// and the constraint attaining it (-1 if none).
 template <typename T, int ND>
-OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol) {
-  constexpr int N1 = ND + 1, NA = ND + 1;
-  // feasible start: raise the last coordinate by the largest violation
-  T viol = T(0);
-  int first = -1;
+OPYX_D T max_violation(const Inst<T, ND>& in, const T* y, int* arg) {
+  T worst = -INFINITY;
+  *arg = -1;
   for (int k = 0; k < in.nsub; ++k) {
     const int64_t l = in.jrow[k];
     if (!in.irow[l]) continue;
-    const T r = adot<T, ND>(in.v + l * ND, x) - in.brow[l];
-    if (r > viol) { viol = r; first = (int)l; }
+    const T r = adot<T, ND>(in.v + l * ND, y) - in.brow[l];
+    if (r > worst) { worst = r; *arg = (int)l; }
   }
+  return worst;
+}
+
+// Projection of one instance.  Returns false when the method did not finish
+// within maxiter steps (the last iterate is kept, as the reference does).
+//
+// Tolerances: `tol` (the reference's 1e-9) bounds the ratio test and the
+// descent test in FP64.  FP32 iterates use precision-scaled bounds instead:
+// at degenerate vertices (several constraints through one point, as where a
+// piecewise-linear function is flat) the ratio of a tight constraint rounds
+// to about -1e-8, which an absolute 1e-9 would wrongly read as "behind the
+// step" and step through it.  A claimed KKT point is accepted only if it is
+// feasible to the same precision; otherwise the instance is reported as
+// not converged.
+template <typename T, int ND>
+OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol) {
+  constexpr int N1 = ND + 1, NA = ND + 1;
+  constexpr T eps = sizeof(T) == 4 ? T(1.1920929e-7) : T(2.220446049250313e-16);
+  const T tol_s = fmax(tol, T(64) * eps);           // step-fraction tolerance
+  T xs = T(1);
+#pragma unroll
+  for (int k = 0; k < N1; ++k) xs = fmax(xs, fabs(x[k]));
+  const T tol_feas = T(64) * eps * xs;              // feasibility, absolute
+  // feasible start: raise the last coordinate by the largest violation
+  int first;
+  const T viol = max_violation<T, ND>(in, x, &first);
 #pragma unroll
   for (int k = 0; k < N1; ++k) y[k] = x[k];
-  if (first < 0) return true;     // feasible points are their own projection
+  if (first < 0 || !(viol > T(0))) return true;  // feasible points are fixed
   y[ND] += viol;
   int W[NA];
   T aw[NA][ND];
@@ -178,6 +202,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     int blocking = -1;
     if (m < NA && pn > T(0)) {
       // the nearest constraint outside W that the step would cross
+      const T tol_ap = fmax(tol, T(4) * eps * pn);
       T smin = T(1);
       for (int k = 0; k < in.nsub; ++k) {
         const int64_t l = in.jrow[k];
@@ -188,9 +213,9 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
         if (act) continue;
         const T* vl = in.v + l * ND;
         const T ap = adot<T, ND>(vl, p);
-        if (ap > tol) {
+        if (ap > tol_ap) {
           const T s = (in.brow[l] - adot<T, ND>(vl, y)) / ap;
-          if (s < smin && s > -tol) { smin = s; blocking = (int)l; }
+          if (s < smin && s > -tol_s) { smin = s; blocking = (int)l; }
         }
       }
       if (smin != T(0)) {
@@ -216,7 +241,12 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
 #pragma unroll
     for (int a = 0; a < NA; ++a)
       if (a < m && z[a] < lmin) { lmin = z[a]; amin = a; }
-    if (amin < 0) return true;   // KKT point of the full problem
+    if (amin < 0) {
+      // a KKT point of the working set; it solves the full problem if it is
+      // feasible (else a step crossed a constraint: reported, not hidden)
+      int lv;
+      return !(max_violation<T, ND>(in, y, &lv) > tol_feas);
+    }
     // drop the most negative multiplier
     --m;
     W[amin] = W[m];
