@@ -175,6 +175,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
 #pragma unroll
   for (int k = 0; k < N1; ++k) xs = fmax(xs, fabs(x[k]));
   const T tol_feas = T(64) * eps * xs;              // feasibility, absolute
+  const T tol_tight = T(8) * eps * xs;              // a constraint counts as tight
   // feasible start: raise the last coordinate by the largest violation
   int first;
   const T viol = max_violation<T, ND>(in, x, &first);
@@ -188,6 +189,10 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
   W[0] = first;
 #pragma unroll
   for (int k = 0; k < ND; ++k) aw[0][k] = in.v[first * ND + k];
+  // the constraint dropped last: its negative multiplier says the next step
+  // leaves it, so it does not take part in that step's ratio test (in FP32
+  // a short step's direction is noisy enough to read as "into" it)
+  int dropped = -1;
   for (int it = 0; it < maxiter; ++it) {
     // step: the part of x - y orthogonal to the active normals
     T d[N1], p[N1], z[NA];
@@ -196,33 +201,57 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     ActiveBasis<T, ND> basis;
     if (!basis.build(aw, m)) return false;
     basis.project_out(d, p);
-    T pn = T(0);
+    T pn = T(0), dn = T(0);
 #pragma unroll
-    for (int k = 0; k < N1; ++k) pn += fabs(p[k]);
+    for (int k = 0; k < N1; ++k) { pn += fabs(p[k]); dn += fabs(d[k]); }
     int blocking = -1;
-    if (m < NA && pn > T(0)) {
-      // the nearest constraint outside W that the step would cross
+    bool null_step = false;
+    // a step at the rounding level of its own computation (|p| against
+    // |x - y|) or below the tightness tolerance is noise: the multipliers
+    // decide without it (else, at a degenerate vertex that FP32 places 1e-7
+    // off, noise steps are blocked by the vertex's other constraints and
+    // the working set cycles through them)
+    if (m < NA && pn > fmax(tol_tight, T(64) * eps * dn)) {
+      // the nearest constraint outside W that the step would cross.
+      // Constraints tight to within tol_tight block at once (s = 0): at a
+      // degenerate vertex their ratio (slack / a.p) is rounding noise over
+      // a small a.p.  Among the constraints blocking at the smallest step
+      // (tight at the step's end point), the one most opposed to the step
+      // (largest a.p) is taken, which leaves such a vertex in one exchange.
       const T tol_ap = fmax(tol, T(4) * eps * pn);
       T smin = T(1);
-      for (int k = 0; k < in.nsub; ++k) {
-        const int64_t l = in.jrow[k];
-        if (!in.irow[l]) continue;
-        bool act = false;
+      for (int pass = 0; pass < 2; ++pass) {
+        T apb = T(0);
+        for (int k = 0; k < in.nsub; ++k) {
+          const int64_t l = in.jrow[k];
+          if (!in.irow[l]) continue;
+          bool act = (int)l == dropped;
 #pragma unroll
-        for (int a = 0; a < NA; ++a) act |= (a < m && W[a] == (int)l);
-        if (act) continue;
-        const T* vl = in.v + l * ND;
-        const T ap = adot<T, ND>(vl, p);
-        if (ap > tol_ap) {
-          const T s = (in.brow[l] - adot<T, ND>(vl, y)) / ap;
-          if (s < smin && s > -tol_s) { smin = s; blocking = (int)l; }
+          for (int a = 0; a < NA; ++a) act |= (a < m && W[a] == (int)l);
+          if (act) continue;
+          const T* vl = in.v + l * ND;
+          const T ap = adot<T, ND>(vl, p);
+          if (!(ap > tol_ap)) continue;
+          const T slack = in.brow[l] - adot<T, ND>(vl, y);
+          const T s = slack > tol_tight ? slack / ap : T(0);
+          if (!(s > -tol_s)) continue;
+          if (pass == 0) {
+            smin = fmin(smin, s);
+          } else if (smin < T(1) && slack - smin * ap <= tol_tight && ap > apb) {
+            // tight at the step's end point (the ratios themselves carry
+            // errors of eps*|b|/slack, far above eps near a degenerate vertex)
+            apb = ap;
+            blocking = (int)l;
+          }
         }
       }
       if (smin != T(0)) {
 #pragma unroll
         for (int k = 0; k < N1; ++k) y[k] += smin * p[k];
       }
+      null_step = smin == T(0);
     }
+    dropped = -1;
     if (blocking >= 0) {
       W[m] = blocking;
 #pragma unroll
@@ -236,18 +265,28 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     for (int k = 0; k < N1; ++k) d[k] = x[k] - y[k];
     if (m > basis.m && !basis.build(aw, m)) return false;   // a constraint was added
     basis.multipliers(d, z);
+    // a multiplier counts as negative only beyond the rounding of the
+    // multipliers' scale: a zero multiplier at a degenerate vertex that
+    // rounds to -1e-9 would otherwise be dropped and re-added forever
+    T lscale = T(0);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+      if (a < m) lscale = fmax(lscale, fabs(z[a]));
     int amin = -1;
-    T lmin = T(0);
+    T lmin = -T(64) * eps * lscale;
 #pragma unroll
     for (int a = 0; a < NA; ++a)
       if (a < m && z[a] < lmin) { lmin = z[a]; amin = a; }
-    if (amin < 0) {
+    // a constraint that a zero-length step added and the multipliers drop
+    // again leaves y where it is: y is optimal to working precision
+    if (amin < 0 || (null_step && blocking >= 0 && W[amin] == blocking)) {
       // a KKT point of the working set; it solves the full problem if it is
       // feasible (else a step crossed a constraint: reported, not hidden)
       int lv;
       return !(max_violation<T, ND>(in, y, &lv) > tol_feas);
     }
     // drop the most negative multiplier
+    dropped = W[amin];
     --m;
     W[amin] = W[m];
 #pragma unroll
