@@ -2,9 +2,8 @@
 SplitSum of IdentityOp, IndexedMultAdj, MatrixMultR, ScaleOp, GradientOp,
 PositivityFct, IndicatorFct, L1Norms, EpigraphSupp) against the reference's
 own PDHG run of the same model (tests/golden/sublabel_*.npz).
-Bars: FP64 relative L2 <= 1e-10 of x and y after each dumped iteration;
-FP32 <= 1e-4 (the epigraph QP's active sets are decided at the 1e-9
-tolerance of the reference, which FP32 iterates cross differently)."""
+Bars: FP64 relative L2 <= 1e-10 of x and y after each dumped iteration
+(measured ~1e-14); FP32 <= 1e-5 (measured <= 4e-6 after 200 iterations)."""
 
 import numpy as np
 import pytest
@@ -65,9 +64,9 @@ def test_fp64_matches_reference(name):
 def test_fp32_matches_reference(name):
     z = load(name)
     _, rec = run(z, "float")
-    k = len(z["dump_iters"]) - 1
-    x, y, _ = rec[int(z["dump_iters"][k])]
-    assert rel(x, z["x"][k]) <= 1e-4 and rel(y, z["y"][k]) <= 1e-4
+    for k, it in enumerate(z["dump_iters"]):
+        x, y, _ = rec[int(it)]
+        assert rel(x, z["x"][k]) <= 1e-5 and rel(y, z["y"][k]) <= 1e-5, (name, it)
 
 
 def test_envelope_gap_equals_faces_gap():
