@@ -364,6 +364,13 @@ typedef struct {
   void* ws;             /* workspace of opyx_rof_workspace_size() bytes,
                            256-byte aligned, zero-filled once before its
                            first use                                         */
+  void* y2;             /* (N, D, C) or NULL.  Given, 2-D FP32 problems with
+                           constant or preconditioned steps run each
+                           iteration as ONE sweep over HBM (xbar kept on
+                           chip), ping-ponging x <-> xbar and y <-> y2; after
+                           opyx_rof_iterate returns, x and y hold the state
+                           as without it (an odd count ends with one
+                           two-pass iteration)                               */
 } opyx_rof_buffers;
 
 /* Values of the last opyx_rof_gap (pdhg.py:23-44) and of the step state.
@@ -387,7 +394,8 @@ int opyx_rof_init(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* st
 int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
                      void* stream);
 /* One pass of an iteration (0 = primal pass A, 1 = dual pass B, 2 = the
- * adaptive residual pass R), for per-kernel timing and profiling. */
+ * adaptive residual pass R, 3 = one single-sweep iteration (x, y) -> (xbar,
+ * y2), which needs y2), for per-kernel timing and profiling. */
 int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   void* stream);
 /* Allocation-free variant of opyx_rof_init + opyx_rof_iterate (+ opyx_rof_gap).

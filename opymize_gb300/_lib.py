@@ -88,7 +88,7 @@ class opyx_rof_problem(C.Structure):
 class opyx_rof_buffers(C.Structure):
     _fields_ = [("x", C.c_void_p), ("xbar", C.c_void_p), ("y", C.c_void_p),
                 ("f", C.c_void_p), ("mask", C.c_void_p), ("xgrad", C.c_void_p),
-                ("gp", C.c_void_p), ("ws", C.c_void_p)]
+                ("gp", C.c_void_p), ("ws", C.c_void_p), ("y2", C.c_void_p)]
 
 
 class opyx_rof_info(C.Structure):

@@ -7,6 +7,7 @@
 #include "rof_kernels.cuh"
 #include "rof_vec.cuh"
 #include "rof_pipe.cuh"
+#include "rof_sweep.cuh"
 
 namespace opyx {
 namespace rof {
@@ -130,6 +131,8 @@ static Args<T> make_args(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   a.mask = b->mask;
   a.xgrad = (T*)b->xgrad;
   a.gp = (T*)b->gp;
+  a.x2 = (T*)b->xbar;
+  a.y2 = (T*)b->y2;
   char* ws = (char*)b->ws;
   a.st = (opyx_adaptive_state*)(ws + kStateOff);
   a.info = (opyx_rof_info*)(ws + kInfoOff);
@@ -262,6 +265,47 @@ struct PipeLaunch<float, D, C> {
   }
 };
 
+// Single-sweep iterations (rof_sweep.cuh): 2-D FP32 problems with constant
+// or preconditioned steps whose caller gave the second dual buffer y2.
+template <typename T, int D>
+static bool sweep_ok(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  return D == 2 && p->steps != OPYX_STEPS_ADAPTIVE && b->y2 && !(((uintptr_t)b->y2) & 15) &&
+         pipe_ok<T>(p, b);
+}
+
+template <typename T, int D, int C>
+struct SweepLaunch {
+  static void run(const Geo<T>&, const Args<T>&, cudaStream_t) {}
+};
+
+template <int C>
+struct SweepLaunch<float, 2, C> {
+  static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+    constexpr int smem = SweepSmem<C>::bytes;
+    static int per_sm = -1;
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C>, smem);
+    const int64_t gx = (g.nl + kPipeTW - 1) / kPipeTW;
+    const int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
+    int64_t gy = target / gx;
+    if (gy < 1) gy = 1;
+    if (gy > g.rows) gy = g.rows;
+    const int RB = (int)((g.rows + gy - 1) / gy);
+    gy = (g.rows + RB - 1) / RB;
+    k_sweep<C><<<dim3((unsigned)gx, (unsigned)gy, 1), kPipeThreads, smem, s>>>(g, a, RB);
+  }
+};
+
+// Args of the second iteration of a pair: read (xbar, y2), write (x, y).
+template <typename T>
+static Args<T> swapped(const Args<T>& a) {
+  Args<T> b = a;
+  b.x = a.x2;
+  b.x2 = a.x;
+  b.y = a.y2;
+  b.y2 = a.y;
+  return b;
+}
+
 template <typename T, int D, int C>
 struct Runner {
   static int init(const opyx_rof_problem* p, const opyx_rof_buffers* b, cudaStream_t s) {
@@ -309,7 +353,17 @@ struct Runner {
     Args<T> a = make_args<T>(p, b);
     const bool v = vec_ok<T>(p, b), pp = pipe_ok<T>(p, b);
     const int R = rows_per_thread(p, g);
-    for (int it = 0; it < iters; ++it) {
+    int rest = iters;
+    if (sweep_ok<T, D>(p, b)) {
+      // pairs of sweeps return the state to (x, y); an odd count ends with
+      // one two-pass iteration in place
+      const Args<T> a2 = swapped(a);
+      for (; rest >= 2; rest -= 2) {
+        SweepLaunch<T, D, C>::run(g, a, s);
+        SweepLaunch<T, D, C>::run(g, a2, s);
+      }
+    }
+    for (int it = 0; it < rest; ++it) {
       launch(p, g, a, 0, v, R, s, pp);
       launch(p, g, a, 1, v, R, s, pp);
       if (p->steps == OPYX_STEPS_ADAPTIVE) launch(p, g, a, 2, v, R, s, pp);
@@ -319,10 +373,15 @@ struct Runner {
 
   static int pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   cudaStream_t s) {
-    if (which < 0 || which > 2 || (which == 2 && p->steps != OPYX_STEPS_ADAPTIVE))
+    if (which < 0 || which > 3 || (which == 2 && p->steps != OPYX_STEPS_ADAPTIVE))
       return OPYX_ERR_ARG;
+    if (which == 3 && !sweep_ok<T, D>(p, b)) return OPYX_ERR_UNSUPPORTED;
     Geo<T> g = make_geo<T>(p);
     Args<T> a = make_args<T>(p, b);
+    if (which == 3) {
+      SweepLaunch<T, D, C>::run(g, a, s);
+      return check_launch();
+    }
     launch(p, g, a, which, vec_ok<T>(p, b), rows_per_thread(p, g), s, pipe_ok<T>(p, b));
     return check_launch();
   }
@@ -487,6 +546,7 @@ extern "C" int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void
   b.xbar = base + round256(kWsBytes);
   b.xgrad = nfields > 1 ? base + round256(kWsBytes) + field : nullptr;
   b.gp = nfields > 1 ? base + round256(kWsBytes) + 2 * field : nullptr;
+  b.y2 = nullptr;
   // opyx_rof_init clears the info record and the reduction ticket, which the
   // previous call left behind, and rewrites the step state.
   st = opyx_rof_init(p, &b, stream);

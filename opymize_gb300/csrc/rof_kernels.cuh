@@ -95,6 +95,8 @@ struct Args {
   const uint8_t* mask;
   T* xgrad;
   T* gp;
+  T* x2;   // single-sweep iterations: targets of x and y (ping-pong)
+  T* y2;
   opyx_adaptive_state* st;
   double* partials;
   unsigned* ticket;

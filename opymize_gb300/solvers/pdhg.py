@@ -188,6 +188,10 @@ class PDHG(object):
         gp = DeviceArray.empty((N * C,), dtype) if adaptive else None
         wsb = lib.opyx_rof_workspace_size()
         ws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
+        # second dual buffer: 2-D FP32 iterations then run as one sweep over
+        # HBM each (the library falls back to two passes where it cannot)
+        y2 = DeviceArray.empty((y.size,), dtype) \
+            if dtype == np.float32 and D == 2 and not adaptive else None
         p = self._rof_problem(dtype, steps)
         b = _lib.opyx_rof_buffers()
         b.x, b.xbar, b.y, b.f = x.ptr, xbar.ptr, y.ptr, fdev.ptr
@@ -195,8 +199,9 @@ class PDHG(object):
         b.xgrad = None if xgrad is None else xgrad.ptr
         b.gp = None if gp is None else gp.ptr
         b.ws = ws.ptr
+        b.y2 = None if y2 is None else y2.ptr
         self._fused = dict(x=x, y=y, xbar=xbar, f=fdev, mask=mask, xgrad=xgrad, gp=gp, ws=ws,
-                           problem=p, buffers=b)
+                           y2=y2, problem=p, buffers=b)
         if pd_res_mode:
             p.term_mode = 2
         else:
@@ -408,8 +413,13 @@ class _FusedLoop(object):
             _lib.call("opyx_rof_iterate", self.p, self.b, n, stream_ptr())
             if check:
                 _lib.call("opyx_rof_gap", self.p, self.b, stream_ptr())
-        per_it = 3 if self.p.steps == _lib.STEPS["adaptive"] else 2
-        self.launches += n * per_it + (1 if check else 0)
+        p = self.p
+        if self.b.y2 and p.ndim == 2 and p.dtype == _lib.OPYX_F32 and \
+                p.steps != _lib.STEPS["adaptive"] and not (p.flags & 3):
+            kernels = (n // 2) * 2 + (n % 2) * 2       # sweeps; an odd count ends two-pass
+        else:
+            kernels = n * (3 if p.steps == _lib.STEPS["adaptive"] else 2)
+        self.launches += kernels + (1 if check else 0)
 
     def run(self, maxiter, depth=DEPTH, on_check=None, interrupted=None):
         """Iterate until the stop test passes at a check, `maxiter` iterations

@@ -263,3 +263,53 @@ def test_fused_matches_oracle_on_large_colour_problem():
     assert rel(s.state[0], so.state[0]) <= 1e-12
     assert rel(s.state[1], so.state[1]) <= 1e-12
     assert abs(s.info["relgap"] - so.info["relgap"]) <= 1e-10
+
+
+@pytest.mark.parametrize("dims,C,huber,steps,masked", [((512, 384), 3, 0.01, "precond", False),
+                                                        ((200, 132), 1, 0.0, "const", True),
+                                                        ((67, 1024), 2, 0.02, "precond", True),
+                                                        ((1, 516), 4, 0.0, "precond", False),
+                                                        ((2048, 8), 3, 0.01, "const", False)])
+@pytest.mark.parametrize("iters", [1, 6, 7])
+def test_single_sweep_matches_two_passes_bitwise(dims, C, huber, steps, masked, iters):
+    """2-D FP32 iterations as one sweep over HBM (second dual buffer y2 given)
+    against the two-pass row-streaming kernels: the same arithmetic per pixel,
+    so the iterates must agree bit for bit -- for even counts (pairs of
+    sweeps), odd counts (pairs + one two-pass tail), ragged tiles and rows,
+    masks, constant and preconditioned steps, and across CTA row runs."""
+    from opymize_gb300 import _lib
+    from opymize_gb300.gpuarray import DeviceArray, stream_ptr
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG
+    f = piecewise_constant(dims, C, sigma=0.1, seed=4)
+    N, D = int(np.prod(dims)), len(dims)
+    mask = (np.random.default_rng(2).random(N) > 0.2) if masked else None
+    Fg = HuberL1Norms(N, (C, D), 0.07, huber) if huber > 0 else L1Norms(N, (C, D), 0.07)
+    s = PDHG(SSD(f.reshape(N, C), mask=mask), Fg, GradientOp(dims, C, scheme="forward"))
+    s.constvars.update(theta=1.0, tau=0.3, sigma=0.4)
+    out = []
+    for sweep in (False, True):
+        p = s._rof_problem(np.float32, steps)
+        x = DeviceArray.zeros((N * C,), np.float32)
+        y = DeviceArray.zeros((N * D * C,), np.float32)
+        xbar = DeviceArray.zeros((N * C,), np.float32)
+        y2 = DeviceArray.zeros((N * D * C,), np.float32)
+        ws = DeviceArray.zeros(((_lib.load().opyx_rof_workspace_size() + 7) // 8,), np.float64)
+        fd = s.g.f_dev(np.float32)
+        md = s.g.mask_dev()
+        b = _lib.opyx_rof_buffers()
+        b.x, b.xbar, b.y, b.f, b.ws = x.ptr, xbar.ptr, y.ptr, fd.ptr, ws.ptr
+        b.mask = None if md is None else md.ptr
+        b.y2 = y2.ptr if sweep else None
+        _lib.call("opyx_rof_init", p, b, stream_ptr())
+        # start from a nonzero point: a few two-pass iterations first
+        b2 = _lib.opyx_rof_buffers.from_buffer_copy(b)
+        b2.y2 = None
+        _lib.call("opyx_rof_iterate", p, b2, 3, stream_ptr())
+        _lib.call("opyx_rof_iterate", p, b, iters, stream_ptr())
+        out.append((x.get().copy(), y.get().copy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.abs(out[1][1]).max() > 0
