@@ -225,11 +225,11 @@ struct PipeLaunch {
 };
 
 template <typename K>
-static int pipe_blocks_per_sm(K kernel, int smem) {
+static int pipe_blocks_per_sm(K kernel, int smem, int threads = kPipeThreads) {
   int n = 0;
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kPipeThreads, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess)
     return 0;
   return n;
 }
@@ -283,7 +283,7 @@ struct SweepLaunch<float, 2, C> {
   static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
     constexpr int smem = SweepSmem<C>::bytes;
     static int per_sm = -1;
-    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C>, smem);
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C>, smem, kSweepThreads);
     const int64_t gx = (g.nl + kPipeTW - 1) / kPipeTW;
     const int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
     int64_t gy = target / gx;
@@ -291,7 +291,7 @@ struct SweepLaunch<float, 2, C> {
     if (gy > g.rows) gy = g.rows;
     const int RB = (int)((g.rows + gy - 1) / gy);
     gy = (g.rows + RB - 1) / RB;
-    k_sweep<C><<<dim3((unsigned)gx, (unsigned)gy, 1), kPipeThreads, smem, s>>>(g, a, RB);
+    k_sweep<C><<<dim3((unsigned)gx, (unsigned)gy, 1), kSweepThreads, smem, s>>>(g, a, RB);
   }
 };
 

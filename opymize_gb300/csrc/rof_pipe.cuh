@@ -40,7 +40,7 @@ OPYX_D void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "mem
 // holding pixels [q_beg - HL, q_beg + TW + HR).  Chunks outside the row or
 // outside [0, rows) are zero-filled; `need` = false (a row past the end of
 // the CTA's run) issues nothing.
-template <int E, int HL, int HR>
+template <int E, int HL, int HR, int NT = kPipeThreads>
 OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float>& g, int64_t r,
                      int64_t q_beg, bool need = true) {
   if (!need) return;
@@ -50,7 +50,7 @@ OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float
   const int64_t row_f0 = (rv ? r : 0) * g.nl * E;        // float offset of the row
   const int64_t f0 = (q_beg - HL) * E;                    // float offset of the slot in the row
   const int64_t fmax = g.nl * E;
-  for (int c = threadIdx.x; c < NCH; c += kPipeThreads) {
+  for (int c = threadIdx.x; c < NCH; c += NT) {
     const int64_t fo = f0 + (int64_t)c * 4;
     const bool valid = rv && fo >= 0 && fo + 4 <= fmax;
     cp_async16(slot + c * 4, arr + row_f0 + (valid ? fo : 0), valid);
@@ -59,7 +59,7 @@ OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float
 
 // Cooperative coalesced store of the first TW pixels (after HL halo pixels)
 // of a slot to row r.
-template <int E, int HL>
+template <int E, int HL, int NT = kPipeThreads>
 OPYX_D void store_row(float* __restrict__ arr, const float* slot, const Geo<float>& g, int64_t r,
                       int64_t q_beg) {
   constexpr int NCH = kPipeTW * E / 4;
@@ -67,7 +67,7 @@ OPYX_D void store_row(float* __restrict__ arr, const float* slot, const Geo<floa
   const int64_t fmax = g.nl * E;
   float* row = arr + r * g.nl * E;
   const float4* s = reinterpret_cast<const float4*>(slot + HL * E);
-  for (int c = threadIdx.x; c < NCH; c += kPipeThreads) {
+  for (int c = threadIdx.x; c < NCH; c += NT) {
     const int64_t fo = f0 + (int64_t)c * 4;
     if (fo + 4 <= fmax) *reinterpret_cast<float4*>(row + fo) = s[c];
   }
