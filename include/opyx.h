@@ -377,11 +377,13 @@ typedef struct {
  * `checks` counts the gap evaluations since opyx_rof_init; `done` becomes 1
  * at the first one that passes the stop test of the problem's term_mode,
  * after which every opyx_rof_* kernel returns at once (so the host may queue
- * iterations ahead of its checks). */
+ * iterations ahead of its checks).  `fault` becomes 1 (and `done` with it)
+ * if a kernel gave up a bounded wait for its own asynchronous copies; the
+ * iterates are then not valid. */
 typedef struct {
   double objp, objd, infeasp, infeasd, gap, relgap;
   double tau, sigma, alpha, resp, resd, epsp, epsd;
-  double checks, done;
+  double checks, done, fault;
 } opyx_rof_info;
 
 size_t opyx_rof_workspace_size(void);

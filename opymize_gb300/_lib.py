@@ -15,6 +15,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libopyx.so")
 
 OPYX_OK = 0
+OPYX_ERR_LAUNCH = 2
 OPYX_F32, OPYX_F64 = 0, 1
 SCHEME = {"forward": 0, "centered": 1}
 BC = {"neumann": 0, "curvature": 1, "second-order": 2}
@@ -94,7 +95,7 @@ class opyx_rof_buffers(C.Structure):
 class opyx_rof_info(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("objp", "objd", "infeasp", "infeasd", "gap", "relgap", "tau", "sigma",
-                 "alpha", "resp", "resd", "epsp", "epsd", "checks", "done")]
+                 "alpha", "resp", "resd", "epsp", "epsd", "checks", "done", "fault")]
 
 
 ROF_INFO_FIELDS = [n for n, _ in opyx_rof_info._fields_]

@@ -18,8 +18,13 @@
 // is that of k_passA_p / k_passB_p, so results are bit-identical to the two
 // passes.
 //
-// Shared memory per CTA (TW = 512): y ring 3 x (TW+8) x K (4-pixel halo
-// both sides), x and f rings 2 x (TW+4) x C (right halo), xbar 2 x (TW+4) x C.
+// Rows move in and out as 1-D bulk asynchronous copies (TMA) issued by one
+// thread: loads complete on an mbarrier (two, alternating per stage; every
+// wait is bounded and a timeout sets info->fault and ends the kernel),
+// stores are bulk groups drained before their slot is refilled.  The other
+// threads only compute.  Shared memory per CTA (TW = 512): y ring 3 x (TW+8)
+// x K (4-pixel halo both sides), x and f rings 2 x (TW+4) x C (right halo),
+// xbar 2 x (TW+4) x C.
 // Requirements as rof_pipe.cuh (checked on the host); 2-D only (the
 // neighbour one plane away in 3-D would need a plane of xbar on chip).
 #pragma once
@@ -123,12 +128,102 @@ OPYX_D void sweep_a(const Geo<float>& g, const Args<float>& a, const PrimalCoefs
   }
 }
 
+// ---- bulk asynchronous copies (TMA, 1-D) and their mbarriers
+constexpr int kMbarSpin = 1 << 22;   // bound on mbarrier polls (each may suspend)
+
+OPYX_D unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+OPYX_D void mbar_init(uint64_t* m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+OPYX_D void mbar_arrive_expect(uint64_t* m, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)),
+               "r"(bytes) : "memory");
+}
+OPYX_D bool mbar_try(uint64_t* m, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(m)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of parity `parity`; false if the bound ran out.
+OPYX_D bool mbar_wait(uint64_t* m, unsigned parity) {
+  for (int i = 0; i < kMbarSpin; ++i)
+    if (mbar_try(m, parity)) return true;
+  return false;
+}
+OPYX_D void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* m) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(m)) : "memory");
+}
+OPYX_D void bulk_store(void* dst, const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"(smem_u32(src)), "r"(bytes) : "memory");
+}
+OPYX_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+OPYX_D void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+OPYX_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+OPYX_D void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// The in-image part of row r for a slot holding pixels [q_beg - HL,
+// q_beg + TW + HR): bytes (0 if the row is outside the image), the first
+// pixel's offset in the slot and its index in the array.  Slot pixels
+// outside the image are left as they are: every use of them in the sweep is
+// masked by the boundary tests.  Sizes and addresses are multiples of 16
+// bytes because the last axis is a multiple of 4 and the arrays 16-byte
+// aligned (checked on the host).
+template <int E, int HL, int HR>
+OPYX_D unsigned row_span(const Geo<float>& g, int64_t r, int64_t q_beg, int* off_px,
+                         int64_t* src_px) {
+  if (r < 0 || r >= g.rows) return 0u;
+  const int64_t lo_slot = q_beg - HL;
+  const int64_t lo = lo_slot > 0 ? lo_slot : 0;
+  const int64_t hi_slot = q_beg + kPipeTW + HR;
+  const int64_t hi = hi_slot < g.nl ? hi_slot : g.nl;
+  if (hi <= lo) return 0u;
+  *off_px = (int)(lo - lo_slot);
+  *src_px = r * g.nl + lo;
+  return (unsigned)((hi - lo) * E * 4);
+}
+
+// Thread 0: announce and issue the copies of one stage (rows for y, x, f).
+template <int C>
+OPYX_D void issue_stage(const Geo<float>& g, const Args<float>& a, int64_t q_beg, uint64_t* m,
+                        float* ys0, int64_t ry0, float* ys1, int64_t ry1, float* xsl, float* fsl,
+                        int64_t rx) {
+  constexpr int M = 2 * C;
+  int oy0 = 0, oy1 = 0, ox = 0, of = 0;
+  int64_t sy0 = 0, sy1 = 0, sx = 0, sf = 0;
+  const unsigned by0 = ys0 ? row_span<M, 4, 4>(g, ry0, q_beg, &oy0, &sy0) : 0u;
+  const unsigned by1 = ys1 ? row_span<M, 4, 4>(g, ry1, q_beg, &oy1, &sy1) : 0u;
+  const unsigned bx = row_span<C, 0, 4>(g, rx, q_beg, &ox, &sx);
+  const unsigned bf = row_span<C, 0, 4>(g, rx, q_beg, &of, &sf);
+  mbar_arrive_expect(m, by0 + by1 + bx + bf);
+  if (by0) bulk_load(ys0 + oy0 * M, a.y + sy0 * M, by0, m);
+  if (by1) bulk_load(ys1 + oy1 * M, a.y + sy1 * M, by1, m);
+  if (bx) bulk_load(xsl + ox * C, a.x + sx * C, bx, m);
+  if (bf) bulk_load(fsl + of * C, a.f + sf * C, bf, m);
+}
+
+// Thread 0: store the TW pixels of a slot (after HL halo pixels) to row r.
+template <int E, int HL>
+OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64_t r,
+                       int64_t q_beg) {
+  const int64_t hi = q_beg + kPipeTW < g.nl ? q_beg + kPipeTW : g.nl;
+  if (hi <= q_beg) return;
+  fence_proxy_async();   // the threads' shared-memory writes, before the copy reads them
+  bulk_store(arr + (r * g.nl + q_beg) * E, slot + HL * E, (unsigned)((hi - q_beg) * E * 4));
+  bulk_commit();
+}
+
 template <int C>
 __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
   using S = SweepSmem<C>;
   constexpr int D = 2, M = D * C, P = kSweepP, NT = kSweepThreads;
   extern __shared__ float4 smem4[];
+  __shared__ __align__(8) uint64_t mbar[2];
   float* sm = reinterpret_cast<float*>(smem4);
   float* ys = sm;                          // 3 x Y44: row q in slot (q - r0 + 1) % 3
   float* xs = ys + 3 * S::Y44;             // 2 x X4 : x_k, then x_{k+1}
@@ -136,29 +231,55 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
   float* bs = fs + 2 * S::X4;              // 2 x X4 : xbar rows, slot (q - r0) & 1
   const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
   const int lp0 = threadIdx.x * P;
+  const bool lead = threadIdx.x == 0;        // issues the bulk copies
   const bool halo = threadIdx.x == NT - 1;   // also computes xbar at pixel TW
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const PrimalCoefs<float, C> pc(g, (float)a.tau);
   const float sig_c = (float)a.sigma;
   const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
+  if (lead) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned st = 0;   // stages issued so far; stage s uses mbar[s & 1], parity (s >> 1) & 1
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
     const int64_t rl = r1 < g.rows ? r1 : r1 - 1;   // last row whose pass A runs here
-    copy_row<M, 4, 4, NT>(ys, a.y, g, r0 - 1, q_beg);
-    copy_row<M, 4, 4, NT>(ys + S::Y44, a.y, g, r0, q_beg);
-    copy_row<C, 0, 4, NT>(xs, a.x, g, r0, q_beg);
-    copy_row<C, 0, 4, NT>(fs, a.f, g, r0, q_beg);
-    cp_commit();
+    if (lead) {
+      bulk_wait_read_all();
+      fence_proxy_async();
+      issue_stage<C>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
+    }
+    unsigned cur = st++;
     for (int64_t r = r0; r <= r1; ++r) {
       const int k = (int)(r - r0);
       const bool run_a = r <= rl;
       const bool more = r + 1 <= rl;
-      copy_row<M, 4, 4, NT>(ys + ((k + 2) % 3) * S::Y44, a.y, g, r + 1, q_beg, more);
-      copy_row<C, 0, 4, NT>(xs + ((k + 1) & 1) * S::X4, a.x, g, r + 1, q_beg, more);
-      copy_row<C, 0, 4, NT>(fs + ((k + 1) & 1) * S::X4, a.f, g, r + 1, q_beg, more);
-      cp_commit();
-      cp_wait<1>();
-      __syncthreads();
+      unsigned nxt = cur;
+      if (more) {
+        if (lead) {
+          bulk_wait_read_all();   // stores still reading the slots about to be refilled
+          fence_proxy_async();
+          issue_stage<C>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
+                         r + 1, xs + ((k + 1) & 1) * S::X4, fs + ((k + 1) & 1) * S::X4, r + 1);
+        }
+        nxt = st++;
+      }
+      bool ok = true;
+      if (run_a) ok = mbar_wait(&mbar[cur & 1], (cur >> 1) & 1u);
+      if (__syncthreads_or(!ok)) {
+        // a copy did not arrive within the bound: flag it, give the copies
+        // in flight a bounded chance to land, and leave
+        if (lead) {
+          a.info->fault = 1.0;
+          a.info->done = 1.0;
+          if (more) mbar_wait(&mbar[nxt & 1], (nxt >> 1) & 1u);
+          bulk_wait_all();
+        }
+        return;
+      }
       const float* yc = ys + ((k + 1) % 3) * S::Y44;    // y_k row r
       float* yu = ys + (k % 3) * S::Y44;                // y_k row r - 1
       float* xv = xs + (k & 1) * S::X4;
@@ -183,7 +304,7 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
         }
       }
       __syncthreads();
-      if (r < r1) store_row<C, 0, NT>(a.x2, xv, g, r, q_beg);
+      if (lead && r < r1) store_span<C, 0>(a.x2, xv, g, r, q_beg);
       // ---- pass B, row r - 1 (as k_passB_p), in place in its y slot
       if (r > r0) {
         const int64_t rb = r - 1;
@@ -226,13 +347,13 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
         }
         sts(yu + (lp0 + 4) * M, qy);
         __syncthreads();
-        store_row<M, 4, NT>(a.y2, yu, g, rb, q_beg);
+        if (lead) store_span<M, 4>(a.y2, yu, g, rb, q_beg);
       }
       __syncthreads();
+      cur = nxt;
     }
-    cp_wait<0>();
-    __syncthreads();
   }
+  if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }
 
 }  // namespace rof

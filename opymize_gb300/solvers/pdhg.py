@@ -431,7 +431,8 @@ class _FusedLoop(object):
         nrec = len(_lib.ROF_INFO_FIELDS)
         if self.host is None or self.host.shape[0] < depth + 1:
             self.host = t.empty((depth + 1, nrec), dtype=t.float64, pin_memory=True)
-        i_checks, i_done = nrec - 2, nrec - 1
+        names = _lib.ROF_INFO_FIELDS
+        i_checks, i_done, i_fault = names.index("checks"), names.index("done"), names.index("fault")
         pending = []          # (event, slot) of queued checks, oldest first
         check_iters = []      # iteration count at each queued check
         state = {"rec": None, "checks": 0}
@@ -440,6 +441,9 @@ class _FusedLoop(object):
             ev, slot = pending.pop(0)
             ev.synchronize()
             rec = self.host[slot].numpy().copy()
+            if rec[i_fault] != 0.0:
+                raise _lib.OpyxError("fused PDHG iteration", _lib.OPYX_ERR_LAUNCH,
+                                     "a kernel gave up waiting for its own copies")
             c = int(rec[i_checks])
             if c > state["checks"]:      # checks after the stop returned at once
                 state["checks"], state["rec"] = c, rec

@@ -74,7 +74,9 @@ def test_kernels_return_after_stop():
     off = _lib.load().opyx_rof_info_offset() // 8
     nrec = len(_lib.ROF_INFO_FIELDS)
     rec0 = fz["ws"][off:off + nrec].get().copy()
-    assert rec0[-2] == 1 and rec0[-1] == 1           # one check, stopped
+    names = _lib.ROF_INFO_FIELDS
+    assert rec0[names.index("checks")] == 1 and rec0[names.index("done")] == 1  # stopped
+    assert rec0[names.index("fault")] == 0
     _lib.call("opyx_rof_iterate", fz["problem"], fz["buffers"], 7, stream_ptr())
     _lib.call("opyx_rof_gap", fz["problem"], fz["buffers"], stream_ptr())
     np.testing.assert_array_equal(fz["x"].get(), x0)
