@@ -228,17 +228,21 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """Per-launch DRAM bytes of the fused passes from the committed ncu
-    summary (profiles/rof_passes_2048x2048x3.txt), if present."""
-    path = os.path.join(ROOT, "profiles", "rof_passes_2048x2048x3.txt")
+    """Per-launch DRAM bytes of the fused kernels from the committed ncu
+    summaries (profiles/*.txt lines `traffic_bytes_per_launch <kernel> <bytes>`)."""
     out = {}
+    pdir = os.path.join(ROOT, "profiles")
     try:
-        for line in open(path):
+        names = sorted(os.listdir(pdir))
+    except OSError:
+        return out
+    for fn in names:
+        if not fn.endswith(".txt"):
+            continue
+        for line in open(os.path.join(pdir, fn)):
             if line.startswith("traffic_bytes_per_launch"):
                 _, name, val = line.split()
                 out[name] = float(val)
-    except OSError:
-        pass
     return out
 
 
