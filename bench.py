@@ -42,7 +42,7 @@ UNIT = "ms"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="opyx", choices=["opyx", "reference"])
     ap.add_argument("--size", type=int, default=2048)
@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--gran", type=int, default=6)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the volume and sublabel configurations")
     return ap.parse_args()
 
 
@@ -62,8 +64,8 @@ def workload_config(a, world):
                     "until relgap<=%g" % (a.size, a.size, a.channels, a.huber, a.lbd, a.tol),
         "image": [a.size, a.size, a.channels], "lambda": a.lbd, "huber_alpha": a.huber,
         "steps": "precond", "tol": a.tol, "gap_check_every": a.gran, "seed": a.seed,
-        "l2": "working set (x, xbar, y, f = %d MB) larger than L2" %
-              (4 * a.size * a.size * a.channels * 5 // 2 ** 20),
+        "l2": "working set (x, xbar, y, y2, f = %d MB) larger than L2 (126 MB)" %
+              (4 * a.size * a.size * a.channels * 7 // 2 ** 20),
         "parallelism": "replicas x%d" % world,
     }
 
@@ -96,7 +98,7 @@ class ClockSampler(object):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -108,7 +110,11 @@ class ClockSampler(object):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) == 7:
-                self.rows.append(parts)
+                self.rows.append((time.time(), parts))
+
+    def mark(self):
+        """Host time stamp of the timed region's start or end."""
+        return time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -119,44 +125,51 @@ class ClockSampler(object):
                 self.proc.kill()
             self.t.join(timeout=2)
 
-    def summary(self):
-        if not self.rows:
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and throttle reasons of the samples taken between
+        host times t0 and t1 (the timed region)."""
+        rows = [r for (t, r) in self.rows if (t0 is None or t >= t0) and (t1 is None or t <= t1)]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace('.', '', 1).isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace('.', '', 1).isdigit()]
+        sm = [float(r[0]) for r in rows if r[0].replace('.', '', 1).isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[j] for r in self.rows for j in range(4)
+        reasons = sorted({names[j] for r in rows for j in range(4)
                           if r[3 + j].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(rows)}
 
 
 # ----------------------------------------------------------------- GPU arm
 class ResidentSolver(object):
     """The fused ROF solve with f, x, y, xbar and the workspace resident in HBM."""
 
-    def __init__(self, a, f):
+    def __init__(self, a, f, dims=None, lbd=None, huber=None, gran=None):
         from opymize_gb300 import _lib
         from opymize_gb300.gpuarray import DeviceArray
-        from opymize_gb300.functionals import SSD, HuberL1Norms
+        from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
         from opymize_gb300.linear import GradientOp
         from opymize_gb300.solvers import PDHG
         self.lib = _lib
-        n, C = a.size, a.channels
-        N = n * n
-        self.N, self.C, self.K = N, C, 2 * C
-        self.gran, self.tol = a.gran, a.tol
-        self.solver = PDHG(SSD(f.reshape(N, C)), HuberL1Norms(N, (C, 2), a.lbd, a.huber),
-                           GradientOp((n, n), C, scheme="forward"))
+        dims = (a.size, a.size) if dims is None else tuple(dims)
+        C = f.shape[-1]
+        D = len(dims)
+        N = int(np.prod(dims))
+        lbd = a.lbd if lbd is None else lbd
+        huber = a.huber if huber is None else huber
+        self.N, self.C, self.K = N, C, D * C
+        self.gran, self.tol = (a.gran if gran is None else gran), a.tol
+        F = HuberL1Norms(N, (C, D), lbd, huber) if huber > 0 else L1Norms(N, (C, D), lbd)
+        self.solver = PDHG(SSD(f.reshape(N, C)), F, GradientOp(dims, C, scheme="forward"))
         s = self.solver
         s.constvars.update(theta=1.0, precond=True)
         self.p = s._rof_problem(np.float32, "precond")
         self.f = s.g.f_dev(np.float32)
         self.x = DeviceArray.zeros((N * C,), np.float32)
-        self.y = DeviceArray.zeros((N * 2 * C,), np.float32)
+        self.y = DeviceArray.zeros((N * D * C,), np.float32)
         self.xbar = DeviceArray.zeros((N * C,), np.float32)
-        self.y2 = DeviceArray.zeros((N * 2 * C,), np.float32)   # single-sweep ping-pong
+        self.y2 = DeviceArray.zeros((N * D * C,), np.float32)   # single-sweep ping-pong (2-D)
         wsb = _lib.load().opyx_rof_workspace_size()
         self.ws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
         b = _lib.opyx_rof_buffers()
@@ -198,6 +211,65 @@ class ResidentSolver(object):
         e1.record(s)
         t.cuda.synchronize()
         return e0.elapsed_time(e1) / reps * 1e-3   # seconds per launch
+
+
+def volume_case(a):
+    """The volume configuration: 256^3, one channel, TV (lambda = 0.08),
+    ellipsoids + noise 0.1, precond steps, until relgap <= 1e-4, data resident
+    (3-D runs the two-pass row-streaming kernels)."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    t = torch()
+    f = piecewise_constant((256, 256, 256), 1, sigma=0.1, seed=a.seed)
+    rs = ResidentSolver(a, f, dims=(256, 256, 256), lbd=0.08, huber=0.0, gran=10)
+    rs.solve()
+    e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    reps = 3
+    t.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        rs.solve()
+    e1.record()
+    t.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    N, C, K = rs.N, rs.C, rs.K
+    it_bytes = 4.0 * N * (5 * C + 3 * K)
+    tA, tB = rs.time_pass(0), rs.time_pass(1)
+    return {"workload": "TV volume 256^3 fp32, lambda=0.08, precond steps, until relgap<=1e-4",
+            "time_to_gap_ms": round(ms, 3), "iters_to_gap": rs.iters, "final_relgap": rs.relgap,
+            "passA_us": round(tA * 1e6, 2), "passB_us": round(tB * 1e6, 2),
+            "iteration_GBps": round(it_bytes / (tA + tB) / 1e9, 1),
+            "data": "synthetic ellipsoids, resident in HBM"}
+
+
+def sublabel_case(a, iters=200):
+    """The sublabel-lifted configuration: 512^2, 16 labels on [0, 1],
+    rho = min((u - f)^2, 0.04) sampled at 8 points per interval, 10%
+    salt-and-pepper, TV weight 0.1, FP32 generic PDHG path with precond
+    steps; iterations per second over `iters` iterations (gap at the end)."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.tools import lifting
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    t = torch()
+    img = np.clip(piecewise_constant((512, 512), 1, sigma=0.05, seed=a.seed,
+                                     salt_pepper=0.1)[..., 0], 0, 1)
+    g, f, A, _ = lifting.sublabel_problem(img, L=16, lbd=0.1, samples=8)
+    s = PDHG(g, f, A)
+    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=20,
+            granularity=20)
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=iters,
+            granularity=iters)
+    t.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return {"workload": "sublabel lifting 512^2, 16 labels, 8 samples/interval, fp32, "
+                        "generic PDHG path, precond steps",
+            "iters_per_s": round(iters / el, 1), "iters": iters,
+            "relgap_after": s.info.get("relgap"),
+            "qp_nonconverged": f.fcts[-1].conj.prox(1.0).nonconverged,
+            "note": "wall time of solve() incl. setup of steps and one final gap"}
 
 
 def e2e_solve(a, f):
@@ -277,22 +349,27 @@ def run_gpu_arm(a, world, rank, local):
         dist.init_process_group("nccl", device_id=t.device("cuda", local))
     f = make_image(a)
     rs = ResidentSolver(a, f)
-    for _ in range(max(3, a.warmup)):
-        rs.solve()
     s = t.cuda.current_stream()
-    launches0 = rs.launches
     e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    # the sampler starts before the warm-up (nvidia-smi takes a while to give
+    # its first line); only samples inside the timed region are kept
     with ClockSampler(local) as clk:
+        for _ in range(max(3, a.warmup)):
+            rs.solve()
+        launches0 = rs.launches
         if dist:
             dist.barrier()
         t.cuda.synchronize()
+        t_start = clk.mark()
         e0.record(s)
         for _ in range(a.steps):
             rs.solve()
         e1.record(s)
         t.cuda.synchronize()
+        t_end = clk.mark()
         if dist:
             dist.barrier()
+    clocks = clk.summary(t_start, t_end)
     ms = e0.elapsed_time(e1) / a.steps
     launches = rs.launches - launches0
     if dist:
@@ -338,6 +415,7 @@ def run_gpu_arm(a, world, rank, local):
         e2e_ms = float(v.item())
 
     out = None
+    rs_iters = rs.iters
     if rank == 0:
         out = {
             "metric": METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world,
@@ -351,17 +429,22 @@ def run_gpu_arm(a, world, rank, local):
                     "api": "PDHG(SSD, HuberL1Norms, GradientOp).solve(use_gpu=True, "
                            "steps='precond', precision='float')"},
             "roofline": roof,
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "gpu_launches": int(launches),
         }
+        if world == 1 and not a.no_extra:
+            # the other configurations of the path, outside the headline metric
+            del rs
+            out["other_workloads"] = {"volume_256x256x256": volume_case(a),
+                                      "sublabel_512x512_L16": sublabel_case(a)}
         if world == 1 and not a.no_cpu:
-            cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs.iters)
+            cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs_iters)
             out["cpu_baseline"] = {
                 "value": round(cpu_ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
                 "sample": "oracle PDHG (numpy/scipy port of the reference CPU path, FP64) on "
                           "the same 2048x2048x3 input: 4 iterations (%.3f s/it) and one gap "
                           "evaluation (%.3f s) timed, scaled to the %d iterations and %d gap "
-                          "checks of the solve" % (t_iter, t_gap, rs.iters, rs.iters // a.gran),
+                          "checks of the solve" % (t_iter, t_gap, rs_iters, rs_iters // a.gran),
                 "host_cpus": os.cpu_count()}
     if dist:
         dist.barrier()
