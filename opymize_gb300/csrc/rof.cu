@@ -237,13 +237,14 @@ static int pipe_blocks_per_sm(K kernel, int smem, int threads = kPipeThreads) {
 template <int D, int C>
 struct PipeLaunch<float, D, C> {
   // Grid: ceil(nl / TW) tiles across x; enough row runs for one full wave
-  // of resident CTAs.
-  template <typename K>
+  // of resident CTAs.  Rows of at most 256 pixels use 256-pixel tiles (64
+  // threads), so no CTA carries an idle half.
+  template <int TW, typename K>
   static void go(K kernel, int smem, const Geo<float>& g, const Args<float>& a, bool reduce,
                  double shift, cudaStream_t s, int which) {
     static int per_sm[3] = {-1, -1, -1};
-    if (per_sm[which] < 0) per_sm[which] = pipe_blocks_per_sm(kernel, smem);
-    const int64_t gx = (g.nl + kPipeTW - 1) / kPipeTW;
+    if (per_sm[which] < 0) per_sm[which] = pipe_blocks_per_sm(kernel, smem, TW / 4);
+    const int64_t gx = (g.nl + TW - 1) / TW;
     int64_t target = (int64_t)(per_sm[which] > 0 ? per_sm[which] : 1) * sm_count();
     if (reduce && target > kMaxBlocks) target = kMaxBlocks;
     int64_t gy = target / gx;
@@ -252,16 +253,22 @@ struct PipeLaunch<float, D, C> {
     const int RB = (int)((g.rows + gy - 1) / gy);
     gy = (g.rows + RB - 1) / RB;
     const dim3 grid((unsigned)gx, (unsigned)gy, 1);
-    if (which == 0) k_passA_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB);
-    else if (which == 1) k_passB_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB);
-    else k_gap_p<D, C><<<grid, kPipeThreads, smem, s>>>(g, a, RB, shift);
+    if (which == 0) k_passA_p<D, C, TW><<<grid, TW / 4, smem, s>>>(g, a, RB);
+    else if (which == 1) k_passB_p<D, C, TW><<<grid, TW / 4, smem, s>>>(g, a, RB);
+    else k_gap_p<D, C, TW><<<grid, TW / 4, smem, s>>>(g, a, RB, shift);
+  }
+  template <int TW>
+  static void run_tw(const Geo<float>& g, const Args<float>& a, int which, double shift,
+                     cudaStream_t s) {
+    using S = PipeSmem<D, C, TW>;
+    if (which == 0) go<TW>(k_passA_p<D, C, TW>, S::A, g, a, false, shift, s, 0);
+    else if (which == 1) go<TW>(k_passB_p<D, C, TW>, S::B, g, a, false, shift, s, 1);
+    else go<TW>(k_gap_p<D, C, TW>, S::G, g, a, true, shift, s, 2);
   }
   static void run(const Geo<float>& g, const Args<float>& a, int which, double shift,
                   cudaStream_t s) {
-    using S = PipeSmem<D, C>;
-    if (which == 0) go(k_passA_p<D, C>, S::A, g, a, false, shift, s, 0);
-    else if (which == 1) go(k_passB_p<D, C>, S::B, g, a, false, shift, s, 1);
-    else go(k_gap_p<D, C>, S::G, g, a, true, shift, s, 2);
+    if (g.nl <= 256) run_tw<256>(g, a, which, shift, s);
+    else run_tw<kPipeTW>(g, a, which, shift, s);
   }
 };
 

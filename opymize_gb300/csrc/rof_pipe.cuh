@@ -40,11 +40,11 @@ OPYX_D void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "mem
 // holding pixels [q_beg - HL, q_beg + TW + HR).  Chunks outside the row or
 // outside [0, rows) are zero-filled; `need` = false (a row past the end of
 // the CTA's run) issues nothing.
-template <int E, int HL, int HR, int NT = kPipeThreads>
+template <int E, int HL, int HR, int NT = kPipeThreads, int TW = kPipeTW>
 OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float>& g, int64_t r,
                      int64_t q_beg, bool need = true) {
   if (!need) return;
-  constexpr int NPX = kPipeTW + HL + HR;
+  constexpr int NPX = TW + HL + HR;
   constexpr int NCH = NPX * E / 4;
   const bool rv = r >= 0 && r < g.rows;
   const int64_t row_f0 = (rv ? r : 0) * g.nl * E;        // float offset of the row
@@ -59,10 +59,10 @@ OPYX_D void copy_row(float* slot, const float* __restrict__ arr, const Geo<float
 
 // Cooperative coalesced store of the first TW pixels (after HL halo pixels)
 // of a slot to row r.
-template <int E, int HL, int NT = kPipeThreads>
+template <int E, int HL, int NT = kPipeThreads, int TW = kPipeTW>
 OPYX_D void store_row(float* __restrict__ arr, const float* slot, const Geo<float>& g, int64_t r,
                       int64_t q_beg) {
-  constexpr int NCH = kPipeTW * E / 4;
+  constexpr int NCH = TW * E / 4;
   const int64_t f0 = q_beg * E;
   const int64_t fmax = g.nl * E;
   float* row = arr + r * g.nl * E;
@@ -80,13 +80,13 @@ OPYX_D void pipe_row_coords(const Geo<float>& g, int64_t r, int64_t* crow, int64
 }
 
 // Shared-memory sizes (bytes) of the three kernels.
-template <int D, int C>
+template <int D, int C, int TW = kPipeTW>
 struct PipeSmem {
   static constexpr int M = D * C;
-  static constexpr int X4 = (kPipeTW + 4) * C;   // floats of a slot with a 4-pixel halo
-  static constexpr int Y4 = (kPipeTW + 4) * M;
-  static constexpr int X0 = kPipeTW * C;
-  static constexpr int Y0 = kPipeTW * M;
+  static constexpr int X4 = (TW + 4) * C;   // floats of a slot with a 4-pixel halo
+  static constexpr int Y4 = (TW + 4) * M;
+  static constexpr int X0 = TW * C;
+  static constexpr int Y0 = TW * M;
   // pass B: xbar ring 3 (halo right), y ring 2, [xbar plane ring 2]
   static constexpr int B = 4 * (3 * X4 + 2 * Y0 + (D == 3 ? 2 * X0 : 0));
   // pass A: y ring 3 (halo left), x ring 2, f ring 2, xbar out, [y plane ring 2]
@@ -96,17 +96,18 @@ struct PipeSmem {
 };
 
 // ------------------------------------------------------------------ pass B
-template <int D, int C>
-__global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<float> a, int RB) {
+template <int D, int C, int TW = kPipeTW>
+__global__ void __launch_bounds__(TW / 4) k_passB_p(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
-  using S = PipeSmem<D, C>;
+  using S = PipeSmem<D, C, TW>;
+  constexpr int NT = TW / 4;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   float* xs = sm;                          // 3 x X4
   float* ys = xs + 3 * S::X4;              // 2 x Y0
   float* zs = ys + 2 * S::Y0;              // 2 x X0 (D = 3)
-  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const int lp0 = threadIdx.x * 4;         // first local pixel of this thread
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const float sig_c = (float)a.sigma;
@@ -114,18 +115,18 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
   const int64_t nplane = D == 3 ? g.n[1] : 0;  // rows per plane
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    copy_row<C, 0, 4>(xs, a.xbar, g, r0, q_beg);
-    copy_row<C, 0, 4>(xs + S::X4, a.xbar, g, r0 + 1, q_beg);
-    copy_row<M, 0, 0>(ys, a.y, g, r0, q_beg);
-    if (D == 3) copy_row<C, 0, 0>(zs, a.xbar, g, r0 + nplane, q_beg);
+    copy_row<C, 0, 4, NT, TW>(xs, a.xbar, g, r0, q_beg);
+    copy_row<C, 0, 4, NT, TW>(xs + S::X4, a.xbar, g, r0 + 1, q_beg);
+    copy_row<M, 0, 0, NT, TW>(ys, a.y, g, r0, q_beg);
+    if (D == 3) copy_row<C, 0, 0, NT, TW>(zs, a.xbar, g, r0 + nplane, q_beg);
     cp_commit();
     for (int64_t r = r0; r < r1; ++r) {
       const int k = (int)(r - r0);
       // prefetch the rows of the next step
-      copy_row<C, 0, 4>(xs + ((k + 2) % 3) * S::X4, a.xbar, g, r + 2, q_beg, r + 2 <= r1);
-      copy_row<M, 0, 0>(ys + ((k + 1) & 1) * S::Y0, a.y, g, r + 1, q_beg, r + 1 < r1);
+      copy_row<C, 0, 4, NT, TW>(xs + ((k + 2) % 3) * S::X4, a.xbar, g, r + 2, q_beg, r + 2 <= r1);
+      copy_row<M, 0, 0, NT, TW>(ys + ((k + 1) & 1) * S::Y0, a.y, g, r + 1, q_beg, r + 1 < r1);
       if (D == 3)
-        copy_row<C, 0, 0>(zs + ((k + 1) & 1) * S::X0, a.xbar, g, r + 1 + nplane, q_beg, r + 1 < r1);
+        copy_row<C, 0, 0, NT, TW>(zs + ((k + 1) & 1) * S::X0, a.xbar, g, r + 1 + nplane, q_beg, r + 1 < r1);
       cp_commit();
       cp_wait<1>();
       __syncthreads();
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
       }
       stv(yv + lp0 * M, qy);
       __syncthreads();
-      store_row<M, 0>(a.y, yv, g, r, q_beg);
+      store_row<M, 0, NT, TW>(a.y, yv, g, r, q_beg);
       __syncthreads();
     }
     cp_wait<0>();
@@ -191,10 +192,11 @@ __global__ void __launch_bounds__(kPipeThreads) k_passB_p(Geo<float> g, Args<flo
 }
 
 // ------------------------------------------------------------------ pass A
-template <int D, int C>
-__global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<float> a, int RB) {
+template <int D, int C, int TW = kPipeTW>
+__global__ void __launch_bounds__(TW / 4) k_passA_p(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
-  using S = PipeSmem<D, C>;
+  using S = PipeSmem<D, C, TW>;
+  constexpr int NT = TW / 4;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
   float* fs = xs + 2 * S::X0;              // 2 x X0
   float* bs = fs + 2 * S::X0;              // 1 x X0 (xbar out)
   float* zs = bs + S::X0;                  // 2 x Y0 (D = 3: y one plane back)
-  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const int lp0 = threadIdx.x * 4;
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   const PrimalCoefs<float, C> pc(g, (float)a.tau);
@@ -211,19 +213,19 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
     // y slot of row r is ((r - r0 + 1) % 3): row r0 - 1 -> 0, r0 -> 1, r0 + 1 -> 2
-    copy_row<M, 4, 0>(ys, a.y, g, r0 - 1, q_beg);
-    copy_row<M, 4, 0>(ys + S::Y4, a.y, g, r0, q_beg);
-    copy_row<C, 0, 0>(xs, a.x, g, r0, q_beg);
-    copy_row<C, 0, 0>(fs, a.f, g, r0, q_beg);
-    if (D == 3) copy_row<M, 0, 0>(zs, a.y, g, r0 - nplane, q_beg);
+    copy_row<M, 4, 0, NT, TW>(ys, a.y, g, r0 - 1, q_beg);
+    copy_row<M, 4, 0, NT, TW>(ys + S::Y4, a.y, g, r0, q_beg);
+    copy_row<C, 0, 0, NT, TW>(xs, a.x, g, r0, q_beg);
+    copy_row<C, 0, 0, NT, TW>(fs, a.f, g, r0, q_beg);
+    if (D == 3) copy_row<M, 0, 0, NT, TW>(zs, a.y, g, r0 - nplane, q_beg);
     cp_commit();
     for (int64_t r = r0; r < r1; ++r) {
       const int k = (int)(r - r0);
       const bool more = r + 1 < r1;
-      copy_row<M, 4, 0>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
-      copy_row<C, 0, 0>(xs + ((k + 1) & 1) * S::X0, a.x, g, r + 1, q_beg, more);
-      copy_row<C, 0, 0>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
-      if (D == 3) copy_row<M, 0, 0>(zs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
+      copy_row<M, 4, 0, NT, TW>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0, NT, TW>(xs + ((k + 1) & 1) * S::X0, a.x, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0, NT, TW>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
+      if (D == 3) copy_row<M, 0, 0, NT, TW>(zs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
       cp_commit();
       cp_wait<1>();
       __syncthreads();
@@ -282,8 +284,8 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
       stv(xv + lp0 * C, qx);
       stv(bs + lp0 * C, qb);
       __syncthreads();
-      store_row<C, 0>(a.x, xv, g, r, q_beg);
-      store_row<C, 0>(a.xbar, bs, g, r, q_beg);
+      store_row<C, 0, NT, TW>(a.x, xv, g, r, q_beg);
+      store_row<C, 0, NT, TW>(a.xbar, bs, g, r, q_beg);
       __syncthreads();
     }
     cp_wait<0>();
@@ -294,11 +296,12 @@ __global__ void __launch_bounds__(kPipeThreads) k_passA_p(Geo<float> g, Args<flo
 // ------------------------------------------------------------------ gap
 // The sums of k_gap; FP32 partials per thread over its pixels and rows,
 // FP64 across threads and blocks.
-template <int D, int C>
-__global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float> a, int RB,
+template <int D, int C, int TW = kPipeTW>
+__global__ void __launch_bounds__(TW / 4) k_gap_p(Geo<float> g, Args<float> a, int RB,
                                                         double ssd_shift) {
   if (stopped(a)) return;
-  using S = PipeSmem<D, C>;
+  using S = PipeSmem<D, C, TW>;
+  constexpr int NT = TW / 4;
   constexpr int M = D * C;
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float
   float* fs = ys + 3 * S::Y4;              // 2 x X0
   float* xzs = fs + 2 * S::X0;             // 2 x X0 (D = 3: x one plane forward)
   float* yzs = xzs + 2 * S::X0;            // 2 x Y0 (D = 3: y one plane back)
-  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const int lp0 = threadIdx.x * 4;
   const int64_t nplane = D == 3 ? g.n[1] : 0;
   double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
@@ -315,25 +318,25 @@ __global__ void __launch_bounds__(kPipeThreads) k_gap_p(Geo<float> g, Args<float
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
     float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;
     // x slot of row r: (r - r0) % 3; y slot of row r: (r - r0 + 1) % 3
-    copy_row<C, 0, 4>(xs, a.x, g, r0, q_beg);
-    copy_row<C, 0, 4>(xs + S::X4, a.x, g, r0 + 1, q_beg);
-    copy_row<M, 4, 0>(ys, a.y, g, r0 - 1, q_beg);
-    copy_row<M, 4, 0>(ys + S::Y4, a.y, g, r0, q_beg);
-    copy_row<C, 0, 0>(fs, a.f, g, r0, q_beg);
+    copy_row<C, 0, 4, NT, TW>(xs, a.x, g, r0, q_beg);
+    copy_row<C, 0, 4, NT, TW>(xs + S::X4, a.x, g, r0 + 1, q_beg);
+    copy_row<M, 4, 0, NT, TW>(ys, a.y, g, r0 - 1, q_beg);
+    copy_row<M, 4, 0, NT, TW>(ys + S::Y4, a.y, g, r0, q_beg);
+    copy_row<C, 0, 0, NT, TW>(fs, a.f, g, r0, q_beg);
     if (D == 3) {
-      copy_row<C, 0, 0>(xzs, a.x, g, r0 + nplane, q_beg);
-      copy_row<M, 0, 0>(yzs, a.y, g, r0 - nplane, q_beg);
+      copy_row<C, 0, 0, NT, TW>(xzs, a.x, g, r0 + nplane, q_beg);
+      copy_row<M, 0, 0, NT, TW>(yzs, a.y, g, r0 - nplane, q_beg);
     }
     cp_commit();
     for (int64_t r = r0; r < r1; ++r) {
       const int k = (int)(r - r0);
       const bool more = r + 1 < r1;
-      copy_row<C, 0, 4>(xs + ((k + 2) % 3) * S::X4, a.x, g, r + 2, q_beg, r + 2 <= r1);
-      copy_row<M, 4, 0>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
-      copy_row<C, 0, 0>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
+      copy_row<C, 0, 4, NT, TW>(xs + ((k + 2) % 3) * S::X4, a.x, g, r + 2, q_beg, r + 2 <= r1);
+      copy_row<M, 4, 0, NT, TW>(ys + ((k + 2) % 3) * S::Y4, a.y, g, r + 1, q_beg, more);
+      copy_row<C, 0, 0, NT, TW>(fs + ((k + 1) & 1) * S::X0, a.f, g, r + 1, q_beg, more);
       if (D == 3) {
-        copy_row<C, 0, 0>(xzs + ((k + 1) & 1) * S::X0, a.x, g, r + 1 + nplane, q_beg, more);
-        copy_row<M, 0, 0>(yzs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
+        copy_row<C, 0, 0, NT, TW>(xzs + ((k + 1) & 1) * S::X0, a.x, g, r + 1 + nplane, q_beg, more);
+        copy_row<M, 0, 0, NT, TW>(yzs + ((k + 1) & 1) * S::Y0, a.y, g, r + 1 - nplane, q_beg, more);
       }
       cp_commit();
       cp_wait<1>();
