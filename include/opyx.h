@@ -400,6 +400,36 @@ int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int i
  * y2), which needs y2), for per-kernel timing and profiling. */
 int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int which,
                   void* stream);
+/* Batched solves (the reference solves one problem per PDHG object; a batch
+ * serves workloads of many independent images, e.g. a data set): 2-D FP32
+ * problems with constant or preconditioned steps, all with the same channel
+ * count, their buffers as for the single sweep (x, xbar, y, y2, f; ws unused).
+ * One launch per iteration covers every active instance.
+ *
+ * records: device array of ninst * opyx_rof_batch_record_bytes() bytes
+ *   (256-aligned): instance i's step state at records + i*512 and its
+ *   opyx_rof_info at records + i*512 + 256 (stop test per instance's
+ *   term_mode, `done`, `fault` as for single solves).
+ * opyx_rof_batch_describe fills, ON THE HOST, a descriptor of
+ *   opyx_rof_batch_desc_bytes(ninst, nitems) bytes: per instance its
+ *   coefficients and pointers, and work items (rows_per_item rows x 512
+ *   pixels) for the instances with active[i] != 0 (all if active is NULL);
+ *   the caller copies it to device memory and passes that copy below.
+ * opyx_rof_batch_init writes every instance's step state and clears its info.
+ * opyx_rof_batch_iterate runs `iters` (even) iterations of the active items.
+ * opyx_rof_batch_gap evaluates the gap of every instance with items, using
+ *   `partials` (device, nitems * 5 doubles). */
+size_t opyx_rof_batch_record_bytes(void);
+size_t opyx_rof_batch_desc_bytes(int ninst, int nitems);
+int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffers* bufs,
+                            int ninst, void* records, const uint8_t* active, int rows_per_item,
+                            void* host_desc, size_t host_bytes, int* nitems);
+int opyx_rof_batch_init(const void* desc, int ninst, void* stream);
+int opyx_rof_batch_iterate(const void* desc, int ninst, int nitems, int nchannels, int iters,
+                           void* stream);
+int opyx_rof_batch_gap(const void* desc, int ninst, int nitems, int nchannels, double* partials,
+                       void* stream);
+
 /* Allocation-free variant of opyx_rof_init + opyx_rof_iterate (+ opyx_rof_gap).
  * It has no counterpart in the reference: it serves callers that cannot
  * allocate device memory (code running inside another framework's memory

@@ -304,7 +304,7 @@ struct SweepLaunch<float, 2, C> {
 
 // Args of the second iteration of a pair: read (xbar, y2), write (x, y).
 template <typename T>
-static Args<T> swapped(const Args<T>& a) {
+static __host__ __device__ Args<T> swapped(const Args<T>& a) {
   Args<T> b = a;
   b.x = a.x2;
   b.x2 = a.x;
@@ -569,3 +569,333 @@ extern "C" int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void
   }
   return OPYX_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched solves: many independent 2-D FP32 problems with constant or
+// preconditioned steps, one launch per iteration for all of them.
+//
+// The host fills a descriptor (opyx_rof_batch_describe): per instance its
+// geometry/coefficients, buffer pointers and step state; a list of work
+// items (instance, row run, 512-pixel column tile) over the active
+// instances.  The sweep kernel walks the items (grid-stride) with the body of
+// the single-instance sweep; small instances then cost a few CTAs instead of
+// a launch each.  Gaps: per-item FP64 partial sums, folded per instance in
+// item order (deterministic) into the instance's info record with the stop
+// test.  Per-instance step state and info records are 512-byte records in
+// one caller array.
+// ---------------------------------------------------------------------------
+namespace opyx {
+namespace rof {
+
+constexpr size_t kBatchRecord = 512;   // [0, 256) step state, [256, 512) info
+
+struct BatchHeader {
+  int32_t ninst, nitems, nchannels, pad;
+};
+
+struct BatchInst {
+  Geo<float> g;
+  Args<float> a;
+  opyx_adaptive_state st0;
+  double ssd_shift;
+  int32_t item_beg, item_end;
+};
+
+struct BatchItem {
+  int32_t inst, r0, r1, q_beg;
+};
+
+static size_t batch_inst_off() { return (sizeof(BatchHeader) + 255) & ~(size_t)255; }
+static size_t batch_item_off(int ninst) {
+  return (batch_inst_off() + (size_t)ninst * sizeof(BatchInst) + 255) & ~(size_t)255;
+}
+
+// Cooperative copy of an instance's geometry and arguments into shared memory.
+OPYX_D void load_inst(const BatchInst* src, BatchInst* dst) {
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  constexpr int nw = (int)(sizeof(BatchInst) / 4);
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
+}
+
+template <int C>
+__global__ void __launch_bounds__(kSweepThreads, 3)
+k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+              int nitems, int flip) {
+  extern __shared__ float4 smem4[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(16) BatchInst cur;
+  float* sm = reinterpret_cast<float*>(smem4);
+  const bool lead = threadIdx.x == 0;
+  if (lead) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned st = 0;
+  int loaded = -1;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BatchItem item = items[it];
+    if (item.inst != loaded) {
+      __syncthreads();   // nobody still reads the previous instance
+      load_inst(&insts[item.inst], &cur);
+      __syncthreads();
+      loaded = item.inst;
+    }
+    if (cur.a.info->done != 0.0) continue;   // uniform: read by every thread alike
+    const Args<float> a = flip ? swapped(cur.a) : cur.a;
+    if (!sweep_rows<C>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
+  }
+  if (lead) bulk_wait_all();
+}
+
+// Per-item partial sums of the gap (as k_gap): {G, |Ax|, G*, |y|^2, max(|y| - lbd)}.
+template <int C>
+__global__ void __launch_bounds__(256)
+k_gap_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+            int nitems, double* partials) {
+  constexpr int D = 2, M = D * C;
+  __shared__ __align__(16) BatchInst cur;
+  __shared__ double red[5][8];
+  int loaded = -1;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BatchItem item = items[it];
+    if (item.inst != loaded) {
+      __syncthreads();
+      load_inst(&insts[item.inst], &cur);
+      __syncthreads();
+      loaded = item.inst;
+    }
+    const Geo<float>& g = cur.g;
+    const Args<float>& a = cur.a;
+    double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
+    if (a.info->done == 0.0) {
+      const int64_t qe = item.q_beg + kPipeTW < g.nl ? item.q_beg + kPipeTW : g.nl;
+      const int64_t w = qe - item.q_beg;
+      const int64_t npx = w * (item.r1 - item.r0);
+      for (int64_t t = threadIdx.x; t < npx; t += blockDim.x) {
+        const int64_t r = item.r0 + t / w, q = item.q_beg + t % w;
+        const int64_t i = r * g.nl + q;
+        int64_t c[3];
+        coords<float, D>(g, r, q, c);
+        float ax[M], div[C];
+        grad_at<float, D, C>(g, a.x, i, c, ax);
+        div_at<float, D, C>(g, a.y, i, c, div);
+        const bool on = !a.mask || a.mask[i];
+        if (on) {
+          float pg = 0.f, ps = 0.f;
+#pragma unroll
+          for (int k = 0; k < C; ++k) {
+            const float fk = a.f[i * C + k];
+            const float d = a.x[i * C + k] - fk;
+            pg += g.vol[k] * d * d;
+            ps += div[k] * div[k] * g.half_rvol[k] - fk * div[k];
+          }
+          sG += 0.5 * (double)pg;
+          sGs += (double)ps;
+        }
+        float n2 = 0.f, y2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+          n2 += ax[j] * ax[j];
+          const float yj = a.y[i * M + j];
+          y2 += yj * yj;
+        }
+        const float nrm = sqrtf(n2);
+        const float fv = g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
+        sF += (double)fv;
+        sFs += (double)y2;
+        inf = fmax(inf, (double)(sqrtf(y2) - g.lbd));
+      }
+    }
+    double v[5] = {sG, sF, sGs, sFs, inf};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      double r = warp_reduce(k == 4 ? RED_MAX : RED_SUM, v[k]);
+      if (lane == 0) red[k][warp] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+      const int k = threadIdx.x;
+      double r = k == 4 ? 0.0 : 0.0;
+      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2)
+        r = k == 4 ? fmax(r, red[k][w2]) : r + red[k][w2];
+      partials[(size_t)it * 5 + k] = r;
+    }
+    __syncthreads();
+  }
+}
+
+// Per instance: fold its items' partials in order and write its info record
+// (objectives, gap, stop test) as the single-instance gap kernels do.
+__global__ void k_gap_fold(const BatchInst* __restrict__ insts, int ninst,
+                           const double* __restrict__ partials) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst) return;
+  const BatchInst& b = insts[i];
+  if (b.item_end <= b.item_beg || b.a.info->done != 0.0) return;
+  double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int it = b.item_beg; it < b.item_end; ++it)
+    for (int k = 0; k < 5; ++k)
+      tot[k] = k == 4 ? fmax(tot[k], partials[(size_t)it * 5 + k]) : tot[k] + partials[(size_t)it * 5 + k];
+  write_info(b.g, b.a, tot, b.ssd_shift);
+}
+
+__global__ void k_batch_init(const BatchInst* __restrict__ insts, int ninst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst) return;
+  *insts[i].a.st = insts[i].st0;
+  opyx_rof_info* info = insts[i].a.info;
+  memset(info, 0, sizeof(opyx_rof_info));
+}
+
+static int batch_check(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  int st = validate(p, b);
+  if (st) return st;
+  if (p->dtype != OPYX_F32 || p->ndim != 2 || p->steps == OPYX_STEPS_ADAPTIVE)
+    return OPYX_ERR_UNSUPPORTED;
+  if (!b->y2 || (((uintptr_t)b->y2) & 15) || !pipe_ok<float>(p, b)) return OPYX_ERR_ARG;
+  if (p->dims[0] > INT32_MAX || p->dims[1] > INT32_MAX) return OPYX_ERR_UNSUPPORTED;
+  return OPYX_OK;
+}
+
+template <int C>
+static int batch_launch_sweep(const BatchInst* insts, const BatchItem* items, int nitems,
+                              int flip, cudaStream_t s) {
+  constexpr int smem = SweepSmem<C>::bytes;
+  static int per_sm = -1;
+  if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep_batch<C>, smem, kSweepThreads);
+  int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
+  if (grid > nitems) grid = nitems;
+  k_sweep_batch<C><<<(unsigned)grid, kSweepThreads, smem, s>>>(insts, items, nitems, flip);
+  return check_launch();
+}
+
+}  // namespace rof
+}  // namespace opyx
+
+extern "C" {
+
+size_t opyx_rof_batch_record_bytes(void) { return kBatchRecord; }
+
+size_t opyx_rof_batch_desc_bytes(int ninst, int nitems) {
+  if (ninst < 0 || nitems < 0) return 0;
+  return batch_item_off(ninst) + (size_t)nitems * sizeof(BatchItem);
+}
+
+int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffers* bufs,
+                            int ninst, void* records, const uint8_t* active, int rows_per_item,
+                            void* host_desc, size_t host_bytes, int* nitems_out) {
+  if (!probs || !bufs || ninst < 1 || !records || rows_per_item < 1 || !host_desc || !nitems_out)
+    return OPYX_ERR_ARG;
+  if (((uintptr_t)records) & 255) return OPYX_ERR_WORKSPACE;
+  const int C = probs[0].nchannels;
+  int64_t nitems = 0;
+  for (int i = 0; i < ninst; ++i) {
+    opyx_rof_buffers bb = bufs[i];
+    bb.ws = records;   // the batch keeps step state and info in `records`
+    int st = batch_check(&probs[i], &bb);
+    if (st) return st;
+    if (probs[i].nchannels != C) return OPYX_ERR_ARG;
+    if (active && !active[i]) continue;
+    const int64_t gx = (probs[i].dims[1] + kPipeTW - 1) / kPipeTW;
+    const int64_t gy = (probs[i].dims[0] + rows_per_item - 1) / rows_per_item;
+    nitems += gx * gy;
+  }
+  if (nitems > INT32_MAX) return OPYX_ERR_UNSUPPORTED;
+  if (host_bytes < opyx_rof_batch_desc_bytes(ninst, (int)nitems)) return OPYX_ERR_WORKSPACE;
+  char* base = (char*)host_desc;
+  BatchHeader* h = (BatchHeader*)base;
+  h->ninst = ninst;
+  h->nitems = (int)nitems;
+  h->nchannels = C;
+  h->pad = 0;
+  BatchInst* insts = (BatchInst*)(base + batch_inst_off());
+  BatchItem* items = (BatchItem*)(base + batch_item_off(ninst));
+  int32_t k = 0;
+  for (int i = 0; i < ninst; ++i) {
+    const opyx_rof_problem* p = &probs[i];
+    BatchInst& bi = insts[i];
+    memset(&bi, 0, sizeof(bi));
+    opyx_rof_buffers bb = bufs[i];
+    bb.ws = records;
+    bi.g = make_geo<float>(p);
+    bi.a = make_args<float>(p, &bb);
+    char* rec = (char*)records + (size_t)i * kBatchRecord;
+    bi.a.st = (opyx_adaptive_state*)rec;
+    bi.a.info = (opyx_rof_info*)(rec + 256);
+    bi.a.partials = nullptr;
+    bi.a.ticket = nullptr;
+    host_state(p, &bi.st0);
+    bi.ssd_shift = p->ssd_shift;
+    bi.item_beg = k;
+    if (!active || active[i]) {
+      const int64_t rows = p->dims[0], nl = p->dims[1];
+      for (int64_t r0 = 0; r0 < rows; r0 += rows_per_item)
+        for (int64_t q = 0; q < nl; q += kPipeTW) {
+          BatchItem& it = items[k++];
+          it.inst = i;
+          it.r0 = (int32_t)r0;
+          it.r1 = (int32_t)(r0 + rows_per_item < rows ? r0 + rows_per_item : rows);
+          it.q_beg = (int32_t)q;
+        }
+    }
+    bi.item_end = k;
+  }
+  *nitems_out = (int)nitems;
+  return OPYX_OK;
+}
+
+int opyx_rof_batch_init(const void* desc, int ninst, void* stream) {
+  if (!desc || ninst < 1) return OPYX_ERR_ARG;
+  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
+  k_batch_init<<<(ninst + 127) / 128, 128, 0, (cudaStream_t)stream>>>(insts, ninst);
+  return check_launch();
+}
+
+int opyx_rof_batch_iterate(const void* desc, int ninst, int nitems, int nchannels, int iters,
+                           void* stream) {
+  if (!desc || ninst < 1 || nitems < 0 || iters < 0 || (iters & 1)) return OPYX_ERR_ARG;
+  if (nitems == 0 || iters == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
+  const BatchItem* items = (const BatchItem*)((const char*)desc + batch_item_off(ninst));
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int it = 0; it < iters; ++it) {
+    int st;
+    switch (nchannels) {
+      case 1: st = batch_launch_sweep<1>(insts, items, nitems, it & 1, s); break;
+      case 2: st = batch_launch_sweep<2>(insts, items, nitems, it & 1, s); break;
+      case 3: st = batch_launch_sweep<3>(insts, items, nitems, it & 1, s); break;
+      case 4: st = batch_launch_sweep<4>(insts, items, nitems, it & 1, s); break;
+      default: return OPYX_ERR_UNSUPPORTED;
+    }
+    if (st) return st;
+  }
+  return OPYX_OK;
+}
+
+int opyx_rof_batch_gap(const void* desc, int ninst, int nitems, int nchannels, double* partials,
+                       void* stream) {
+  if (!desc || ninst < 1 || nitems < 0 || (nitems > 0 && !partials)) return OPYX_ERR_ARG;
+  if (((uintptr_t)partials) & 7) return OPYX_ERR_WORKSPACE;
+  if (nitems == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
+  const BatchItem* items = (const BatchItem*)((const char*)desc + batch_item_off(ninst));
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned grid = (unsigned)(nitems < sm_count() * 8 ? nitems : sm_count() * 8);
+  switch (nchannels) {
+    case 1: k_gap_batch<1><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
+    case 2: k_gap_batch<2><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
+    case 3: k_gap_batch<3><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
+    case 4: k_gap_batch<4><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
+    default: return OPYX_ERR_UNSUPPORTED;
+  }
+  int st = check_launch();
+  if (st) return st;
+  k_gap_fold<<<(ninst + 127) / 128, 128, 0, s>>>(insts, ninst, partials);
+  return check_launch();
+}
+
+}  // extern "C"

@@ -217,19 +217,19 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
   bulk_commit();
 }
 
+// One run of rows [r0, r1) of the column tile at q_beg: the body of the
+// sweep, shared by the single-instance and the batched kernels.  `st` counts
+// the stages this CTA has issued on its two mbarriers.  Returns false if a
+// copy did not arrive within the wait bound (info->fault is then set).
 template <int C>
-__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<float> a, int RB) {
-  if (stopped(a)) return;
+OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
+                       int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
   using S = SweepSmem<C>;
   constexpr int D = 2, M = D * C, P = kSweepP, NT = kSweepThreads;
-  extern __shared__ float4 smem4[];
-  __shared__ __align__(8) uint64_t mbar[2];
-  float* sm = reinterpret_cast<float*>(smem4);
   float* ys = sm;                          // 3 x Y44: row q in slot (q - r0 + 1) % 3
   float* xs = ys + 3 * S::Y44;             // 2 x X4 : x_k, then x_{k+1}
   float* fs = xs + 2 * S::X4;              // 2 x X4
   float* bs = fs + 2 * S::X4;              // 2 x X4 : xbar rows, slot (q - r0) & 1
-  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
   const int lp0 = threadIdx.x * P;
   const bool lead = threadIdx.x == 0;        // issues the bulk copies
   const bool halo = threadIdx.x == NT - 1;   // also computes xbar at pixel TW
@@ -237,6 +237,123 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
   const PrimalCoefs<float, C> pc(g, (float)a.tau);
   const float sig_c = (float)a.sigma;
   const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
+  const int64_t rl = r1 < g.rows ? r1 : r1 - 1;   // last row whose pass A runs here
+  if (lead) {
+    bulk_wait_read_all();
+    fence_proxy_async();
+    issue_stage<C>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
+  }
+  unsigned cur = st++;
+  for (int64_t r = r0; r <= r1; ++r) {
+    const int k = (int)(r - r0);
+    const bool run_a = r <= rl;
+    const bool more = r + 1 <= rl;
+    unsigned nxt = cur;
+    if (more) {
+      if (lead) {
+        bulk_wait_read_all();   // stores still reading the slots about to be refilled
+        fence_proxy_async();
+        issue_stage<C>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
+                       r + 1, xs + ((k + 1) & 1) * S::X4, fs + ((k + 1) & 1) * S::X4, r + 1);
+      }
+      nxt = st++;
+    }
+    bool ok = true;
+    if (run_a) ok = mbar_wait(&mbar[cur & 1], (cur >> 1) & 1u);
+    if (__syncthreads_or(!ok)) {
+      // a copy did not arrive within the bound: flag it, give the copies
+      // in flight a bounded chance to land, and leave
+      if (lead) {
+        a.info->fault = 1.0;
+        a.info->done = 1.0;
+        if (more) mbar_wait(&mbar[nxt & 1], (nxt >> 1) & 1u);
+        bulk_wait_all();
+      }
+      return false;
+    }
+    const float* yc = ys + ((k + 1) % 3) * S::Y44;    // y_k row r
+    float* yu = ys + (k % 3) * S::Y44;                // y_k row r - 1
+    float* xv = xs + (k & 1) * S::X4;
+    const float* fv = fs + (k & 1) * S::X4;
+    float* bc = bs + (k & 1) * S::X4;                 // xbar row r
+    const float* bu = bs + ((k + 1) & 1) * S::X4;     // xbar row r - 1
+    // ---- pass A, row r (and xbar at the first pixel past the tile)
+    if (run_a) {
+      float qx[P * C], qb[P * C];
+      sweep_a<C, P>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, lp0, qx, qb);
+      float hb[C];
+      if (halo) {
+        float hx[C];
+        sweep_a<C, 1>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, kPipeTW, hx, hb);
+      }
+      __syncthreads();   // every thread has read the x_k values it needs
+      sts(xv + lp0 * C, qx);
+      sts(bc + lp0 * C, qb);
+      if (halo) {
+#pragma unroll
+        for (int k2 = 0; k2 < C; ++k2) bc[kPipeTW * C + k2] = hb[k2];
+      }
+    }
+    __syncthreads();
+    if (lead && r < r1) store_span<C, 0>(a.x2, xv, g, r, q_beg);
+    // ---- pass B, row r - 1 (as k_passB_p), in place in its y slot
+    if (r > r0) {
+      const int64_t rb = r - 1;
+      const bool has_next = rb < g.rows - 1;
+      float qx[P * C], qn[P * C], qy[P * M], xr[C];
+      lds(qx, bu + lp0 * C);
+      lds(qn, bc + lp0 * C);
+      lds(qy, yu + (lp0 + 4) * M);
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) xr[k2] = bu[(lp0 + P) * C + k2];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const int64_t q = q_beg + lp0 + p;
+        const bool inx = q < g.nl - 1;
+        float hf[M];
+#pragma unroll
+        for (int k2 = 0; k2 < C; ++k2) {
+          const float xk = qx[p * C + k2];
+          const float nb = p < P - 1 ? qx[(p + 1) * C + k2] : xr[k2];
+          const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
+          qy[p * M + (D - 1) * C + k2] += (pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c) * gl;
+          hf[(D - 1) * C + k2] = pre ? (inx ? g.hub_pre[D - 1][k2] : 1.f) : hub_c;
+          const float gr = has_next ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
+          qy[p * M + (D - 2) * C + k2] +=
+              (pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c) * gr;
+          hf[(D - 2) * C + k2] = pre ? (has_next ? g.hub_pre[D - 2][k2] : 1.f) : hub_c;
+        }
+        if (g.use_huber) {
+#pragma unroll
+          for (int j = 0; j < M; ++j) qy[p * M + j] *= hf[j];
+        }
+        float n2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < M; ++j) n2 += qy[p * M + j] * qy[p * M + j];
+        if (n2 > g.lbd2) {
+          const float sc = g.lbd * rsqrtf(n2);
+#pragma unroll
+          for (int j = 0; j < M; ++j) qy[p * M + j] *= sc;
+        }
+      }
+      sts(yu + (lp0 + 4) * M, qy);
+      __syncthreads();
+      if (lead) store_span<M, 4>(a.y2, yu, g, rb, q_beg);
+    }
+    __syncthreads();
+    cur = nxt;
+  }
+    return true;
+}
+
+template <int C>
+__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<float> a, int RB) {
+  if (stopped(a)) return;
+  extern __shared__ float4 smem4[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const bool lead = threadIdx.x == 0;
   if (lead) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -246,112 +363,7 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
   unsigned st = 0;   // stages issued so far; stage s uses mbar[s & 1], parity (s >> 1) & 1
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    const int64_t rl = r1 < g.rows ? r1 : r1 - 1;   // last row whose pass A runs here
-    if (lead) {
-      bulk_wait_read_all();
-      fence_proxy_async();
-      issue_stage<C>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
-    }
-    unsigned cur = st++;
-    for (int64_t r = r0; r <= r1; ++r) {
-      const int k = (int)(r - r0);
-      const bool run_a = r <= rl;
-      const bool more = r + 1 <= rl;
-      unsigned nxt = cur;
-      if (more) {
-        if (lead) {
-          bulk_wait_read_all();   // stores still reading the slots about to be refilled
-          fence_proxy_async();
-          issue_stage<C>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
-                         r + 1, xs + ((k + 1) & 1) * S::X4, fs + ((k + 1) & 1) * S::X4, r + 1);
-        }
-        nxt = st++;
-      }
-      bool ok = true;
-      if (run_a) ok = mbar_wait(&mbar[cur & 1], (cur >> 1) & 1u);
-      if (__syncthreads_or(!ok)) {
-        // a copy did not arrive within the bound: flag it, give the copies
-        // in flight a bounded chance to land, and leave
-        if (lead) {
-          a.info->fault = 1.0;
-          a.info->done = 1.0;
-          if (more) mbar_wait(&mbar[nxt & 1], (nxt >> 1) & 1u);
-          bulk_wait_all();
-        }
-        return;
-      }
-      const float* yc = ys + ((k + 1) % 3) * S::Y44;    // y_k row r
-      float* yu = ys + (k % 3) * S::Y44;                // y_k row r - 1
-      float* xv = xs + (k & 1) * S::X4;
-      const float* fv = fs + (k & 1) * S::X4;
-      float* bc = bs + (k & 1) * S::X4;                 // xbar row r
-      const float* bu = bs + ((k + 1) & 1) * S::X4;     // xbar row r - 1
-      // ---- pass A, row r (and xbar at the first pixel past the tile)
-      if (run_a) {
-        float qx[P * C], qb[P * C];
-        sweep_a<C, P>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, lp0, qx, qb);
-        float hb[C];
-        if (halo) {
-          float hx[C];
-          sweep_a<C, 1>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, kPipeTW, hx, hb);
-        }
-        __syncthreads();   // every thread has read the x_k values it needs
-        sts(xv + lp0 * C, qx);
-        sts(bc + lp0 * C, qb);
-        if (halo) {
-#pragma unroll
-          for (int k2 = 0; k2 < C; ++k2) bc[kPipeTW * C + k2] = hb[k2];
-        }
-      }
-      __syncthreads();
-      if (lead && r < r1) store_span<C, 0>(a.x2, xv, g, r, q_beg);
-      // ---- pass B, row r - 1 (as k_passB_p), in place in its y slot
-      if (r > r0) {
-        const int64_t rb = r - 1;
-        const bool has_next = rb < g.rows - 1;
-        float qx[P * C], qn[P * C], qy[P * M], xr[C];
-        lds(qx, bu + lp0 * C);
-        lds(qn, bc + lp0 * C);
-        lds(qy, yu + (lp0 + 4) * M);
-#pragma unroll
-        for (int k2 = 0; k2 < C; ++k2) xr[k2] = bu[(lp0 + P) * C + k2];
-#pragma unroll
-        for (int p = 0; p < P; ++p) {
-          const int64_t q = q_beg + lp0 + p;
-          const bool inx = q < g.nl - 1;
-          float hf[M];
-#pragma unroll
-          for (int k2 = 0; k2 < C; ++k2) {
-            const float xk = qx[p * C + k2];
-            const float nb = p < P - 1 ? qx[(p + 1) * C + k2] : xr[k2];
-            const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
-            qy[p * M + (D - 1) * C + k2] += (pre ? (inx ? g.sig_pre[D - 1][k2] : 0.f) : sig_c) * gl;
-            hf[(D - 1) * C + k2] = pre ? (inx ? g.hub_pre[D - 1][k2] : 1.f) : hub_c;
-            const float gr = has_next ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
-            qy[p * M + (D - 2) * C + k2] +=
-                (pre ? (has_next ? g.sig_pre[D - 2][k2] : 0.f) : sig_c) * gr;
-            hf[(D - 2) * C + k2] = pre ? (has_next ? g.hub_pre[D - 2][k2] : 1.f) : hub_c;
-          }
-          if (g.use_huber) {
-#pragma unroll
-            for (int j = 0; j < M; ++j) qy[p * M + j] *= hf[j];
-          }
-          float n2 = 0.f;
-#pragma unroll
-          for (int j = 0; j < M; ++j) n2 += qy[p * M + j] * qy[p * M + j];
-          if (n2 > g.lbd2) {
-            const float sc = g.lbd * rsqrtf(n2);
-#pragma unroll
-            for (int j = 0; j < M; ++j) qy[p * M + j] *= sc;
-          }
-        }
-        sts(yu + (lp0 + 4) * M, qy);
-        __syncthreads();
-        if (lead) store_span<M, 4>(a.y2, yu, g, rb, q_beg);
-      }
-      __syncthreads();
-      cur = nxt;
-    }
+    if (!sweep_rows<C>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }

@@ -1,3 +1,4 @@
-"""Solvers (opymize/solvers)."""
+"""Solvers (opymize/solvers) on libopyx kernels."""
 
 from opymize_gb300.solvers.pdhg import PDHG   # noqa: F401
+from opymize_gb300.solvers.batch import BatchROF   # noqa: F401

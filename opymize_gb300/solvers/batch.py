@@ -1,0 +1,192 @@
+"""Batched ROF-type solves: many independent images, one launch per iteration.
+
+The reference solves one problem per `PDHG` object (opymize/solvers/pdhg.py:
+229-315); workloads of many images (a data set, tiles of a mosaic) then pay a
+full solver set-up and a chain of small launches per image.  `BatchROF` runs
+the fused single-sweep iteration of every active image in one launch (the
+images' tiles form one work list), evaluates every image's gap in one launch
+pair, and retires each image as soon as its own stop test passes (the
+reference's test, pdhg.py:290-305).  The arithmetic per pixel is that of the
+single-image fused path, so an image's iterates are identical to its own
+`PDHG.solve(steps="precond", precision="float")` run.
+
+Restrictions (those of the single sweep): 2-D images whose last axis is a
+multiple of 4, one channel count for the whole batch, FP32, preconditioned
+steps.  The gap check interval must be even (iterations run in pairs).
+"""
+
+import time
+
+import numpy as np
+
+from opymize_gb300 import _lib
+from opymize_gb300.gpuarray import DeviceArray, stream_ptr, torch
+from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+from opymize_gb300.linear import GradientOp
+from opymize_gb300.solvers.pdhg import PDHG, INFO_KEYS
+
+
+class BatchROF(object):
+    """min_x 0.5*|x - f_i|^2 + lbd_i * TV(x) (Huber-smoothed with alpha > 0)
+    for every image f_i of `images` ((H, W) or (H, W, C) arrays)."""
+
+    ROWS_CANDIDATES = (8, 16, 32, 64)
+
+    def __init__(self, images, lbd, huber=0.0, tol=1e-4, granularity=10, rows_per_item=None):
+        if not images:
+            raise ValueError("empty batch")
+        self.n = len(images)
+        lbds = np.broadcast_to(np.asarray(lbd, dtype=np.float64), (self.n,))
+        self.tol = float(tol)
+        self.gran = int(granularity) + (int(granularity) & 1)   # iterations run in pairs
+        self.rows_per_item = rows_per_item
+        lib = _lib.load()
+        self.problems = (_lib.opyx_rof_problem * self.n)()
+        self.buffers = (_lib.opyx_rof_buffers * self.n)()
+        self.dims, self.arrays = [], []
+        C = None
+        for i, img in enumerate(images):
+            img = np.asarray(img)
+            img = img[..., None] if img.ndim == 2 else img
+            if img.ndim != 3:
+                raise ValueError("images must be 2-D (optionally with a channel axis)")
+            H, W, Ci = img.shape
+            C = Ci if C is None else C
+            if Ci != C:
+                raise ValueError("all images of a batch need the same channel count")
+            if W % 4:
+                raise ValueError("the last axis of every image must be a multiple of 4")
+            N = H * W
+            F = HuberL1Norms(N, (C, 2), lbds[i], huber) if huber > 0 else L1Norms(N, (C, 2), lbds[i])
+            s = PDHG(SSD(img.reshape(N, C)), F, GradientOp((H, W), C, scheme="forward"))
+            s.constvars.update(theta=1.0, precond=True)
+            p = s._rof_problem(np.float32, "precond")
+            p.term_mode = 1
+            p.term_relgap = p.term_infeas = self.tol
+            self.problems[i] = p
+            arr = dict(x=DeviceArray.zeros((N * C,), np.float32),
+                       y=DeviceArray.zeros((N * 2 * C,), np.float32),
+                       xbar=DeviceArray.empty((N * C,), np.float32),
+                       y2=DeviceArray.empty((N * 2 * C,), np.float32),
+                       f=s.g.f_dev(np.float32))
+            b = self.buffers[i]
+            b.x, b.xbar, b.y, b.y2, b.f = (arr[k].ptr for k in ("x", "xbar", "y", "y2", "f"))
+            self.arrays.append(arr)
+            self.dims.append((H, W, C))
+        self.C = C
+        self.rec_bytes = lib.opyx_rof_batch_record_bytes()
+        self.records = DeviceArray.zeros((self.n * self.rec_bytes // 8,), np.float64)
+        self.launches = 0
+        self.info = []
+
+    # ------------------------------------------------------------ plumbing
+    def _describe(self, active, rows):
+        lib = _lib.load()
+        act = np.ascontiguousarray(active, dtype=np.uint8)
+        nmax = 0
+        for i in range(self.n):
+            if act[i]:
+                H, W, _ = self.dims[i]
+                nmax += -(-H // rows) * -(-W // 512)
+        nbytes = lib.opyx_rof_batch_desc_bytes(self.n, nmax)
+        host = np.zeros(nbytes, dtype=np.uint8)
+        nitems = _lib.C.c_int(0)
+        _lib.call("opyx_rof_batch_describe", self.problems, self.buffers, self.n,
+                  self.records.ptr, act.ctypes.data, int(rows), host.ctypes.data, nbytes,
+                  _lib.C.byref(nitems))
+        t = torch()
+        dev = t.from_numpy(host).to("cuda")
+        part = DeviceArray.empty((max(1, nitems.value) * 5,), np.float64)
+        return dev, nitems.value, part
+
+    def _reset(self):
+        for arr in self.arrays:
+            arr["x"].fill(0.0)
+            arr["y"].fill(0.0)
+
+    def _iterate(self, desc, nitems, n):
+        _lib.call("opyx_rof_batch_iterate", desc.data_ptr(), self.n, nitems, self.C, n,
+                  stream_ptr())
+        self.launches += n
+
+    def _gap(self, desc, nitems, part):
+        _lib.call("opyx_rof_batch_gap", desc.data_ptr(), self.n, nitems, self.C, part.ptr,
+                  stream_ptr())
+        self.launches += 2
+
+    def _records(self):
+        rec = self.records.get().reshape(self.n, self.rec_bytes // 8)
+        return rec[:, 256 // 8:256 // 8 + len(_lib.ROF_INFO_FIELDS)]
+
+    def autotune(self, iters=4):
+        """Rows per work item: each candidate runs `iters` iterations from the
+        zero start, timed with CUDA events; the fastest is kept and the state
+        reset (the tuning iterations do not count)."""
+        t = torch()
+        best = None
+        active = np.ones(self.n, np.uint8)
+        for rows in self.ROWS_CANDIDATES:
+            desc, nitems, _ = self._describe(active, rows)
+            _lib.call("opyx_rof_batch_init", desc.data_ptr(), self.n, stream_ptr())
+            self._iterate(desc, nitems, 2)            # warm
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            e0.record()
+            self._iterate(desc, nitems, iters)
+            e1.record()
+            t.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best is None or ms < best[0]:
+                best = (ms, rows)
+        self.rows_per_item = best[1]
+        self.tuning = {"rows_per_item": best[1], "ms_per_iteration": best[0] / iters}
+        self._reset()
+        return best[1]
+
+    # ---------------------------------------------------------------- solve
+    def solve(self, maxiter=5000):
+        """Iterate until every image passed its stop test or `maxiter`
+        iterations; returns per image a dict with the reference's info keys
+        and `iter`.  States: `self.state(i)` (x as an (H, W, C) array)."""
+        if self.rows_per_item is None:
+            self.autotune()
+        self._reset()
+        names = _lib.ROF_INFO_FIELDS
+        i_done, i_fault = names.index("done"), names.index("fault")
+        active = np.ones(self.n, np.uint8)
+        iters = np.zeros(self.n, np.int64)
+        last = None
+        desc, nitems, part = self._describe(active, self.rows_per_item)
+        _lib.call("opyx_rof_batch_init", desc.data_ptr(), self.n, stream_ptr())
+        t0 = time.perf_counter()
+        it = 0
+        while it < maxiter and active.any():
+            n = min(self.gran, maxiter - it)
+            n += n & 1
+            self._iterate(desc, nitems, n)
+            it += n
+            self._gap(desc, nitems, part)
+            last = self._records()
+            if (last[:, i_fault] != 0).any():
+                raise _lib.OpyxError("batched PDHG iteration", _lib.OPYX_ERR_LAUNCH,
+                                     "a kernel gave up waiting for its own copies")
+            iters[active != 0] = it
+            done = (last[:, i_done] != 0) & (active != 0)
+            if done.any():
+                active[done] = 0
+                if active.any():
+                    desc, nitems, part = self._describe(active, self.rows_per_item)
+        self.elapsed = time.perf_counter() - t0
+        self.info = []
+        for i in range(self.n):
+            d = {k: float(last[i, names.index(k)]) for k in INFO_KEYS}
+            d["iter"] = int(iters[i])
+            d["converged"] = bool(last[i, i_done] != 0)
+            self.info.append(d)
+        return self.info
+
+    def state(self, i):
+        H, W, C = self.dims[i]
+        return self.arrays[i]["x"].get().reshape(H, W, C)
+
+    def pixels(self):
+        return sum(H * W for H, W, _ in self.dims)
