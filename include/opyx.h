@@ -414,7 +414,8 @@ int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int whic
  *   opyx_rof_batch_desc_bytes(ninst, nitems) bytes: per instance its
  *   coefficients and pointers, and work items (rows_per_item rows x 512
  *   pixels) for the instances with active[i] != 0 (all if active is NULL);
- *   the caller copies it to device memory and passes that copy below.
+ *   the caller copies it to device memory and passes both copies below (the
+ *   host copy for the launch shapes, the device copy to the kernels).
  * opyx_rof_batch_init writes every instance's step state and clears its info.
  * opyx_rof_batch_iterate runs `iters` (even) iterations of the active items.
  * opyx_rof_batch_gap evaluates the gap of every instance with items, using
@@ -424,10 +425,9 @@ size_t opyx_rof_batch_desc_bytes(int ninst, int nitems);
 int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffers* bufs,
                             int ninst, void* records, const uint8_t* active, int rows_per_item,
                             void* host_desc, size_t host_bytes, int* nitems);
-int opyx_rof_batch_init(const void* desc, int ninst, void* stream);
-int opyx_rof_batch_iterate(const void* desc, int ninst, int nitems, int nchannels, int iters,
-                           void* stream);
-int opyx_rof_batch_gap(const void* desc, int ninst, int nitems, int nchannels, double* partials,
+int opyx_rof_batch_init(const void* host_desc, const void* dev_desc, void* stream);
+int opyx_rof_batch_iterate(const void* host_desc, const void* dev_desc, int iters, void* stream);
+int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* partials,
                        void* stream);
 
 /* Allocation-free variant of opyx_rof_init + opyx_rof_iterate (+ opyx_rof_gap).

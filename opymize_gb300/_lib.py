@@ -157,9 +157,9 @@ SIGNATURES = {
     "opyx_rof_batch_desc_bytes": (sz, [i32, i32]),
     "opyx_rof_batch_describe": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), i32, vp, vp, i32,
                                       vp, sz, P(C.c_int)]),
-    "opyx_rof_batch_init": (i32, [vp, i32, vp]),
-    "opyx_rof_batch_iterate": (i32, [vp, i32, i32, i32, i32, vp]),
-    "opyx_rof_batch_gap": (i32, [vp, i32, i32, i32, vp, vp]),
+    "opyx_rof_batch_init": (i32, [vp, vp, vp]),
+    "opyx_rof_batch_iterate": (i32, [vp, vp, i32, vp]),
+    "opyx_rof_batch_gap": (i32, [vp, vp, vp, vp]),
 }
 
 _lib = None

@@ -287,18 +287,25 @@ struct SweepLaunch {
 
 template <int C>
 struct SweepLaunch<float, 2, C> {
-  static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
-    constexpr int smem = SweepSmem<C>::bytes;
+  template <int TW>
+  static void go(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+    constexpr int smem = SweepSmem<C, TW>::bytes;
     static int per_sm = -1;
-    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C>, smem, kSweepThreads);
-    const int64_t gx = (g.nl + kPipeTW - 1) / kPipeTW;
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C, TW>, smem, TW / kSweepP);
+    const int64_t gx = (g.nl + TW - 1) / TW;
     const int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
     int64_t gy = target / gx;
     if (gy < 1) gy = 1;
     if (gy > g.rows) gy = g.rows;
     const int RB = (int)((g.rows + gy - 1) / gy);
     gy = (g.rows + RB - 1) / RB;
-    k_sweep<C><<<dim3((unsigned)gx, (unsigned)gy, 1), kSweepThreads, smem, s>>>(g, a, RB);
+    k_sweep<C, TW><<<dim3((unsigned)gx, (unsigned)gy, 1), TW / kSweepP, smem, s>>>(g, a, RB);
+  }
+  // narrow rows get narrow tiles, so that no CTA carries idle threads
+  static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+    if (g.nl <= 128) go<128>(g, a, s);
+    else if (g.nl <= 256) go<256>(g, a, s);
+    else go<kPipeTW>(g, a, s);
   }
 };
 
@@ -589,8 +596,17 @@ namespace rof {
 
 constexpr size_t kBatchRecord = 512;   // [0, 256) step state, [256, 512) info
 
+// Work items come in three tile-width classes (128, 256, 512 pixels), each
+// image in the narrowest class that holds its rows, so narrow images do not
+// leave most of a 512-pixel CTA idle; the sweep launches once per class.
+constexpr int kBatchClasses = 3;
+constexpr int kBatchTW[kBatchClasses] = {128, 256, 512};
+
+static int batch_class(int64_t nl) { return nl <= 128 ? 0 : nl <= 256 ? 1 : 2; }
+
 struct BatchHeader {
   int32_t ninst, nitems, nchannels, pad;
+  int32_t class_beg[kBatchClasses + 1];   // items of class c: [class_beg[c], class_beg[c+1])
 };
 
 struct BatchInst {
@@ -602,7 +618,7 @@ struct BatchInst {
 };
 
 struct BatchItem {
-  int32_t inst, r0, r1, q_beg;
+  int32_t inst, r0, r1, q_beg, q_end;
 };
 
 static size_t batch_inst_off() { return (sizeof(BatchHeader) + 255) & ~(size_t)255; }
@@ -618,8 +634,8 @@ OPYX_D void load_inst(const BatchInst* src, BatchInst* dst) {
   for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
 }
 
-template <int C>
-__global__ void __launch_bounds__(kSweepThreads, 3)
+template <int C, int TW>
+__global__ void __launch_bounds__(TW / kSweepP, 3 * kPipeTW / TW)
 k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
               int nitems, int flip) {
   extern __shared__ float4 smem4[];
@@ -645,7 +661,7 @@ k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__
     }
     if (cur.a.info->done != 0.0) continue;   // uniform: read by every thread alike
     const Args<float> a = flip ? swapped(cur.a) : cur.a;
-    if (!sweep_rows<C>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();
 }
@@ -671,7 +687,7 @@ k_gap_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ i
     const Args<float>& a = cur.a;
     double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
     if (a.info->done == 0.0) {
-      const int64_t qe = item.q_beg + kPipeTW < g.nl ? item.q_beg + kPipeTW : g.nl;
+      const int64_t qe = item.q_end;
       const int64_t w = qe - item.q_beg;
       const int64_t npx = w * (item.r1 - item.r0);
       for (int64_t t = threadIdx.x; t < npx; t += blockDim.x) {
@@ -761,16 +777,28 @@ static int batch_check(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   return OPYX_OK;
 }
 
-template <int C>
+template <int C, int TW>
 static int batch_launch_sweep(const BatchInst* insts, const BatchItem* items, int nitems,
                               int flip, cudaStream_t s) {
-  constexpr int smem = SweepSmem<C>::bytes;
+  constexpr int smem = SweepSmem<C, TW>::bytes;
   static int per_sm = -1;
-  if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep_batch<C>, smem, kSweepThreads);
+  if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep_batch<C, TW>, smem, TW / kSweepP);
   int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
   if (grid > nitems) grid = nitems;
-  k_sweep_batch<C><<<(unsigned)grid, kSweepThreads, smem, s>>>(insts, items, nitems, flip);
+  k_sweep_batch<C, TW><<<(unsigned)grid, TW / kSweepP, smem, s>>>(insts, items, nitems, flip);
   return check_launch();
+}
+
+template <int C>
+static int batch_sweep_all(const BatchHeader& h, const BatchInst* insts, const BatchItem* items,
+                           int flip, cudaStream_t s) {
+  int st = OPYX_OK;
+  const int n0 = h.class_beg[1] - h.class_beg[0], n1 = h.class_beg[2] - h.class_beg[1];
+  const int n2 = h.class_beg[3] - h.class_beg[2];
+  if (n0) st = batch_launch_sweep<C, 128>(insts, items + h.class_beg[0], n0, flip, s);
+  if (!st && n1) st = batch_launch_sweep<C, 256>(insts, items + h.class_beg[1], n1, flip, s);
+  if (!st && n2) st = batch_launch_sweep<C, 512>(insts, items + h.class_beg[2], n2, flip, s);
+  return st;
 }
 
 }  // namespace rof
@@ -800,7 +828,8 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
     if (st) return st;
     if (probs[i].nchannels != C) return OPYX_ERR_ARG;
     if (active && !active[i]) continue;
-    const int64_t gx = (probs[i].dims[1] + kPipeTW - 1) / kPipeTW;
+    const int64_t tw = kBatchTW[batch_class(probs[i].dims[1])];
+    const int64_t gx = (probs[i].dims[1] + tw - 1) / tw;
     const int64_t gy = (probs[i].dims[0] + rows_per_item - 1) / rows_per_item;
     nitems += gx * gy;
   }
@@ -814,7 +843,6 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
   h->pad = 0;
   BatchInst* insts = (BatchInst*)(base + batch_inst_off());
   BatchItem* items = (BatchItem*)(base + batch_item_off(ninst));
-  int32_t k = 0;
   for (int i = 0; i < ninst; ++i) {
     const opyx_rof_problem* p = &probs[i];
     BatchInst& bi = insts[i];
@@ -830,45 +858,58 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
     bi.a.ticket = nullptr;
     host_state(p, &bi.st0);
     bi.ssd_shift = p->ssd_shift;
-    bi.item_beg = k;
-    if (!active || active[i]) {
-      const int64_t rows = p->dims[0], nl = p->dims[1];
+    bi.item_beg = bi.item_end = 0;
+  }
+  // items grouped by tile class; an image's items are consecutive
+  int32_t k = 0;
+  for (int c = 0; c < kBatchClasses; ++c) {
+    h->class_beg[c] = k;
+    for (int i = 0; i < ninst; ++i) {
+      const opyx_rof_problem* p = &probs[i];
+      if ((active && !active[i]) || batch_class(p->dims[1]) != c) continue;
+      const int64_t rows = p->dims[0], nl = p->dims[1], tw = kBatchTW[c];
+      insts[i].item_beg = k;
       for (int64_t r0 = 0; r0 < rows; r0 += rows_per_item)
-        for (int64_t q = 0; q < nl; q += kPipeTW) {
+        for (int64_t q = 0; q < nl; q += tw) {
           BatchItem& it = items[k++];
           it.inst = i;
           it.r0 = (int32_t)r0;
           it.r1 = (int32_t)(r0 + rows_per_item < rows ? r0 + rows_per_item : rows);
           it.q_beg = (int32_t)q;
+          it.q_end = (int32_t)(q + tw < nl ? q + tw : nl);
         }
+      insts[i].item_end = k;
     }
-    bi.item_end = k;
   }
+  h->class_beg[kBatchClasses] = k;
   *nitems_out = (int)nitems;
   return OPYX_OK;
 }
 
-int opyx_rof_batch_init(const void* desc, int ninst, void* stream) {
-  if (!desc || ninst < 1) return OPYX_ERR_ARG;
-  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
-  k_batch_init<<<(ninst + 127) / 128, 128, 0, (cudaStream_t)stream>>>(insts, ninst);
+int opyx_rof_batch_init(const void* host_desc, const void* dev_desc, void* stream) {
+  if (!host_desc || !dev_desc) return OPYX_ERR_ARG;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1) return OPYX_ERR_ARG;
+  const BatchInst* insts = (const BatchInst*)((const char*)dev_desc + batch_inst_off());
+  k_batch_init<<<(h.ninst + 127) / 128, 128, 0, (cudaStream_t)stream>>>(insts, h.ninst);
   return check_launch();
 }
 
-int opyx_rof_batch_iterate(const void* desc, int ninst, int nitems, int nchannels, int iters,
-                           void* stream) {
-  if (!desc || ninst < 1 || nitems < 0 || iters < 0 || (iters & 1)) return OPYX_ERR_ARG;
-  if (nitems == 0 || iters == 0) return OPYX_OK;
-  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
-  const BatchItem* items = (const BatchItem*)((const char*)desc + batch_item_off(ninst));
+int opyx_rof_batch_iterate(const void* host_desc, const void* dev_desc, int iters, void* stream) {
+  if (!host_desc || !dev_desc || iters < 0 || (iters & 1)) return OPYX_ERR_ARG;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1 || h.nitems < 0) return OPYX_ERR_ARG;
+  if (h.nitems == 0 || iters == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)dev_desc + batch_inst_off());
+  const BatchItem* items = (const BatchItem*)((const char*)dev_desc + batch_item_off(h.ninst));
   cudaStream_t s = (cudaStream_t)stream;
   for (int it = 0; it < iters; ++it) {
     int st;
-    switch (nchannels) {
-      case 1: st = batch_launch_sweep<1>(insts, items, nitems, it & 1, s); break;
-      case 2: st = batch_launch_sweep<2>(insts, items, nitems, it & 1, s); break;
-      case 3: st = batch_launch_sweep<3>(insts, items, nitems, it & 1, s); break;
-      case 4: st = batch_launch_sweep<4>(insts, items, nitems, it & 1, s); break;
+    switch (h.nchannels) {
+      case 1: st = batch_sweep_all<1>(h, insts, items, it & 1, s); break;
+      case 2: st = batch_sweep_all<2>(h, insts, items, it & 1, s); break;
+      case 3: st = batch_sweep_all<3>(h, insts, items, it & 1, s); break;
+      case 4: st = batch_sweep_all<4>(h, insts, items, it & 1, s); break;
       default: return OPYX_ERR_UNSUPPORTED;
     }
     if (st) return st;
@@ -876,16 +917,19 @@ int opyx_rof_batch_iterate(const void* desc, int ninst, int nitems, int nchannel
   return OPYX_OK;
 }
 
-int opyx_rof_batch_gap(const void* desc, int ninst, int nitems, int nchannels, double* partials,
+int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* partials,
                        void* stream) {
-  if (!desc || ninst < 1 || nitems < 0 || (nitems > 0 && !partials)) return OPYX_ERR_ARG;
+  if (!host_desc || !dev_desc) return OPYX_ERR_ARG;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1 || h.nitems < 0 || (h.nitems > 0 && !partials)) return OPYX_ERR_ARG;
   if (((uintptr_t)partials) & 7) return OPYX_ERR_WORKSPACE;
-  if (nitems == 0) return OPYX_OK;
-  const BatchInst* insts = (const BatchInst*)((const char*)desc + batch_inst_off());
-  const BatchItem* items = (const BatchItem*)((const char*)desc + batch_item_off(ninst));
+  if (h.nitems == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)dev_desc + batch_inst_off());
+  const BatchItem* items = (const BatchItem*)((const char*)dev_desc + batch_item_off(h.ninst));
   cudaStream_t s = (cudaStream_t)stream;
+  const int nitems = h.nitems;
   unsigned grid = (unsigned)(nitems < sm_count() * 8 ? nitems : sm_count() * 8);
-  switch (nchannels) {
+  switch (h.nchannels) {
     case 1: k_gap_batch<1><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
     case 2: k_gap_batch<2><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
     case 3: k_gap_batch<3><<<grid, 256, 0, s>>>(insts, items, nitems, partials); break;
@@ -894,7 +938,7 @@ int opyx_rof_batch_gap(const void* desc, int ninst, int nitems, int nchannels, d
   }
   int st = check_launch();
   if (st) return st;
-  k_gap_fold<<<(ninst + 127) / 128, 128, 0, s>>>(insts, ninst, partials);
+  k_gap_fold<<<(h.ninst + 127) / 128, 128, 0, s>>>(insts, h.ninst, partials);
   return check_launch();
 }
 

@@ -34,11 +34,11 @@
 namespace opyx {
 namespace rof {
 
-template <int C>
+template <int C, int TW = kPipeTW>
 struct SweepSmem {
   static constexpr int M = 2 * C;
-  static constexpr int X4 = (kPipeTW + 4) * C;   // right halo
-  static constexpr int Y44 = (kPipeTW + 8) * M;  // 4-pixel halo on both sides
+  static constexpr int X4 = (TW + 4) * C;   // right halo
+  static constexpr int Y44 = (TW + 8) * M;  // 4-pixel halo on both sides
   static constexpr int bytes = 4 * (3 * Y44 + 2 * X4 + 2 * X4 + 2 * X4);
 };
 
@@ -46,7 +46,7 @@ struct SweepSmem {
 // the resident warps of 4-pixel quads at the same shared memory per pixel --
 // the sweep does both passes' arithmetic per byte and is latency-bound.
 constexpr int kSweepP = 2;
-constexpr int kSweepThreads = kPipeTW / kSweepP;
+constexpr int kSweepThreads = kPipeTW / kSweepP;   // of a 512-pixel tile
 
 // Shared <-> register moves of NF consecutive floats: 128-bit when NF is a
 // multiple of 4 (then the address is 16-byte aligned), 64-bit when it is
@@ -173,13 +173,13 @@ OPYX_D void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" 
 // masked by the boundary tests.  Sizes and addresses are multiples of 16
 // bytes because the last axis is a multiple of 4 and the arrays 16-byte
 // aligned (checked on the host).
-template <int E, int HL, int HR>
+template <int E, int HL, int HR, int TW>
 OPYX_D unsigned row_span(const Geo<float>& g, int64_t r, int64_t q_beg, int* off_px,
                          int64_t* src_px) {
   if (r < 0 || r >= g.rows) return 0u;
   const int64_t lo_slot = q_beg - HL;
   const int64_t lo = lo_slot > 0 ? lo_slot : 0;
-  const int64_t hi_slot = q_beg + kPipeTW + HR;
+  const int64_t hi_slot = q_beg + TW + HR;
   const int64_t hi = hi_slot < g.nl ? hi_slot : g.nl;
   if (hi <= lo) return 0u;
   *off_px = (int)(lo - lo_slot);
@@ -188,17 +188,17 @@ OPYX_D unsigned row_span(const Geo<float>& g, int64_t r, int64_t q_beg, int* off
 }
 
 // Thread 0: announce and issue the copies of one stage (rows for y, x, f).
-template <int C>
+template <int C, int TW>
 OPYX_D void issue_stage(const Geo<float>& g, const Args<float>& a, int64_t q_beg, uint64_t* m,
                         float* ys0, int64_t ry0, float* ys1, int64_t ry1, float* xsl, float* fsl,
                         int64_t rx) {
   constexpr int M = 2 * C;
   int oy0 = 0, oy1 = 0, ox = 0, of = 0;
   int64_t sy0 = 0, sy1 = 0, sx = 0, sf = 0;
-  const unsigned by0 = ys0 ? row_span<M, 4, 4>(g, ry0, q_beg, &oy0, &sy0) : 0u;
-  const unsigned by1 = ys1 ? row_span<M, 4, 4>(g, ry1, q_beg, &oy1, &sy1) : 0u;
-  const unsigned bx = row_span<C, 0, 4>(g, rx, q_beg, &ox, &sx);
-  const unsigned bf = row_span<C, 0, 4>(g, rx, q_beg, &of, &sf);
+  const unsigned by0 = ys0 ? row_span<M, 4, 4, TW>(g, ry0, q_beg, &oy0, &sy0) : 0u;
+  const unsigned by1 = ys1 ? row_span<M, 4, 4, TW>(g, ry1, q_beg, &oy1, &sy1) : 0u;
+  const unsigned bx = row_span<C, 0, 4, TW>(g, rx, q_beg, &ox, &sx);
+  const unsigned bf = row_span<C, 0, 4, TW>(g, rx, q_beg, &of, &sf);
   mbar_arrive_expect(m, by0 + by1 + bx + bf);
   if (by0) bulk_load(ys0 + oy0 * M, a.y + sy0 * M, by0, m);
   if (by1) bulk_load(ys1 + oy1 * M, a.y + sy1 * M, by1, m);
@@ -207,10 +207,10 @@ OPYX_D void issue_stage(const Geo<float>& g, const Args<float>& a, int64_t q_beg
 }
 
 // Thread 0: store the TW pixels of a slot (after HL halo pixels) to row r.
-template <int E, int HL>
+template <int E, int HL, int TW>
 OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64_t r,
                        int64_t q_beg) {
-  const int64_t hi = q_beg + kPipeTW < g.nl ? q_beg + kPipeTW : g.nl;
+  const int64_t hi = q_beg + TW < g.nl ? q_beg + TW : g.nl;
   if (hi <= q_beg) return;
   fence_proxy_async();   // the threads' shared-memory writes, before the copy reads them
   bulk_store(arr + (r * g.nl + q_beg) * E, slot + HL * E, (unsigned)((hi - q_beg) * E * 4));
@@ -221,11 +221,11 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
 // sweep, shared by the single-instance and the batched kernels.  `st` counts
 // the stages this CTA has issued on its two mbarriers.  Returns false if a
 // copy did not arrive within the wait bound (info->fault is then set).
-template <int C>
+template <int C, int TW>
 OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
                        int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
-  using S = SweepSmem<C>;
-  constexpr int D = 2, M = D * C, P = kSweepP, NT = kSweepThreads;
+  using S = SweepSmem<C, TW>;
+  constexpr int D = 2, M = D * C, P = kSweepP, NT = TW / kSweepP;
   float* ys = sm;                          // 3 x Y44: row q in slot (q - r0 + 1) % 3
   float* xs = ys + 3 * S::Y44;             // 2 x X4 : x_k, then x_{k+1}
   float* fs = xs + 2 * S::X4;              // 2 x X4
@@ -241,7 +241,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
   if (lead) {
     bulk_wait_read_all();
     fence_proxy_async();
-    issue_stage<C>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
+    issue_stage<C, TW>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
   }
   unsigned cur = st++;
   for (int64_t r = r0; r <= r1; ++r) {
@@ -253,7 +253,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       if (lead) {
         bulk_wait_read_all();   // stores still reading the slots about to be refilled
         fence_proxy_async();
-        issue_stage<C>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
+        issue_stage<C, TW>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
                        r + 1, xs + ((k + 1) & 1) * S::X4, fs + ((k + 1) & 1) * S::X4, r + 1);
       }
       nxt = st++;
@@ -284,18 +284,18 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       float hb[C];
       if (halo) {
         float hx[C];
-        sweep_a<C, 1>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, kPipeTW, hx, hb);
+        sweep_a<C, 1>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, TW, hx, hb);
       }
       __syncthreads();   // every thread has read the x_k values it needs
       sts(xv + lp0 * C, qx);
       sts(bc + lp0 * C, qb);
       if (halo) {
 #pragma unroll
-        for (int k2 = 0; k2 < C; ++k2) bc[kPipeTW * C + k2] = hb[k2];
+        for (int k2 = 0; k2 < C; ++k2) bc[TW * C + k2] = hb[k2];
       }
     }
     __syncthreads();
-    if (lead && r < r1) store_span<C, 0>(a.x2, xv, g, r, q_beg);
+    if (lead && r < r1) store_span<C, 0, TW>(a.x2, xv, g, r, q_beg);
     // ---- pass B, row r - 1 (as k_passB_p), in place in its y slot
     if (r > r0) {
       const int64_t rb = r - 1;
@@ -338,7 +338,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       }
       sts(yu + (lp0 + 4) * M, qy);
       __syncthreads();
-      if (lead) store_span<M, 4>(a.y2, yu, g, rb, q_beg);
+      if (lead) store_span<M, 4, TW>(a.y2, yu, g, rb, q_beg);
     }
     __syncthreads();
     cur = nxt;
@@ -346,13 +346,14 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
     return true;
 }
 
-template <int C>
-__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<float> a, int RB) {
+template <int C, int TW = kPipeTW>
+__global__ void __launch_bounds__(TW / kSweepP, 3 * kPipeTW / TW)
+k_sweep(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
   extern __shared__ float4 smem4[];
   __shared__ __align__(8) uint64_t mbar[2];
   float* sm = reinterpret_cast<float*>(smem4);
-  const int64_t q_beg = blockIdx.x * (int64_t)kPipeTW;
+  const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const bool lead = threadIdx.x == 0;
   if (lead) {
     mbar_init(&mbar[0], 1);
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(Geo<float> g, Args<f
   unsigned st = 0;   // stages issued so far; stage s uses mbar[s & 1], parity (s >> 1) & 1
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    if (!sweep_rows<C>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }

@@ -87,17 +87,20 @@ class BatchROF(object):
         for i in range(self.n):
             if act[i]:
                 H, W, _ = self.dims[i]
-                nmax += -(-H // rows) * -(-W // 512)
+                tw = 128 if W <= 128 else 256 if W <= 256 else 512
+                nmax += -(-H // rows) * -(-W // tw)
         nbytes = lib.opyx_rof_batch_desc_bytes(self.n, nmax)
         host = np.zeros(nbytes, dtype=np.uint8)
         nitems = _lib.C.c_int(0)
+        widths = [self.dims[i][1] for i in range(self.n) if act[i]]
+        self._classes = len({0 if w <= 128 else 1 if w <= 256 else 2 for w in widths})
         _lib.call("opyx_rof_batch_describe", self.problems, self.buffers, self.n,
                   self.records.ptr, act.ctypes.data, int(rows), host.ctypes.data, nbytes,
                   _lib.C.byref(nitems))
         t = torch()
         dev = t.from_numpy(host).to("cuda")
         part = DeviceArray.empty((max(1, nitems.value) * 5,), np.float64)
-        return dev, nitems.value, part
+        return (host, dev), nitems.value, part
 
     def _reset(self):
         for arr in self.arrays:
@@ -105,14 +108,18 @@ class BatchROF(object):
             arr["y"].fill(0.0)
 
     def _iterate(self, desc, nitems, n):
-        _lib.call("opyx_rof_batch_iterate", desc.data_ptr(), self.n, nitems, self.C, n,
+        _lib.call("opyx_rof_batch_iterate", desc[0].ctypes.data, desc[1].data_ptr(), n,
                   stream_ptr())
-        self.launches += n
+        self.launches += n * self._classes
 
     def _gap(self, desc, nitems, part):
-        _lib.call("opyx_rof_batch_gap", desc.data_ptr(), self.n, nitems, self.C, part.ptr,
+        _lib.call("opyx_rof_batch_gap", desc[0].ctypes.data, desc[1].data_ptr(), part.ptr,
                   stream_ptr())
         self.launches += 2
+
+    def _init(self, desc):
+        _lib.call("opyx_rof_batch_init", desc[0].ctypes.data, desc[1].data_ptr(), stream_ptr())
+        self.launches += 1
 
     def _records(self):
         rec = self.records.get().reshape(self.n, self.rec_bytes // 8)
@@ -127,7 +134,7 @@ class BatchROF(object):
         active = np.ones(self.n, np.uint8)
         for rows in self.ROWS_CANDIDATES:
             desc, nitems, _ = self._describe(active, rows)
-            _lib.call("opyx_rof_batch_init", desc.data_ptr(), self.n, stream_ptr())
+            self._init(desc)
             self._iterate(desc, nitems, 2)            # warm
             e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
             e0.record()
@@ -156,7 +163,7 @@ class BatchROF(object):
         iters = np.zeros(self.n, np.int64)
         last = None
         desc, nitems, part = self._describe(active, self.rows_per_item)
-        _lib.call("opyx_rof_batch_init", desc.data_ptr(), self.n, stream_ptr())
+        self._init(desc)
         t0 = time.perf_counter()
         it = 0
         while it < maxiter and active.any():
