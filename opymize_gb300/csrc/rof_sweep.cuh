@@ -48,6 +48,15 @@ struct SweepSmem {
 constexpr int kSweepP = 2;
 constexpr int kSweepThreads = kPipeTW / kSweepP;   // of a 512-pixel tile
 
+// Pixels per thread by channel count: one channel does a third of the
+// arithmetic per row step of three, so its CTAs are made smaller (4 pixels
+// per thread) and twice as many of them overlap their row pipelines on an SM.
+constexpr int sweep_p(int C) { return C == 1 ? 4 : kSweepP; }
+// Resident CTAs per SM the register budget is fitted to.
+constexpr int sweep_min_blocks(int TW, int P) {
+  return (P == 4 ? 6 : 3) * kPipeTW / TW > 32 ? 32 : (P == 4 ? 6 : 3) * kPipeTW / TW;
+}
+
 // Shared <-> register moves of NF consecutive floats: 128-bit when NF is a
 // multiple of 4 (then the address is 16-byte aligned), 64-bit when it is
 // even (8-byte aligned), else one float at a time.
@@ -221,11 +230,11 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
 // sweep, shared by the single-instance and the batched kernels.  `st` counts
 // the stages this CTA has issued on its two mbarriers.  Returns false if a
 // copy did not arrive within the wait bound (info->fault is then set).
-template <int C, int TW>
+template <int C, int TW, int P>
 OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
                        int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
   using S = SweepSmem<C, TW>;
-  constexpr int D = 2, M = D * C, P = kSweepP, NT = TW / kSweepP;
+  constexpr int D = 2, M = D * C, NT = TW / P;
   float* ys = sm;                          // 3 x Y44: row q in slot (q - r0 + 1) % 3
   float* xs = ys + 3 * S::Y44;             // 2 x X4 : x_k, then x_{k+1}
   float* fs = xs + 2 * S::X4;              // 2 x X4
@@ -346,8 +355,8 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
     return true;
 }
 
-template <int C, int TW = kPipeTW>
-__global__ void __launch_bounds__(TW / kSweepP, 3 * kPipeTW / TW)
+template <int C, int TW = kPipeTW, int P = kSweepP>
+__global__ void __launch_bounds__(TW / P, sweep_min_blocks(TW, P))
 k_sweep(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
   extern __shared__ float4 smem4[];
@@ -364,7 +373,7 @@ k_sweep(Geo<float> g, Args<float> a, int RB) {
   unsigned st = 0;   // stages issued so far; stage s uses mbar[s & 1], parity (s >> 1) & 1
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    if (!sweep_rows<C, TW>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW, P>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }
