@@ -289,10 +289,10 @@ template <int C>
 struct SweepLaunch<float, 2, C> {
   template <int TW>
   static void go(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
-    constexpr int smem = SweepSmem<C, TW>::bytes;
-    constexpr int P = sweep_p(C);
+    constexpr int P = sweep_p(C), DP = sweep_depth(C);
+    constexpr int smem = SweepSmem<C, TW, DP>::bytes;
     static int per_sm = -1;
-    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C, TW, P>, smem, TW / P);
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C, TW, P, DP>, smem, TW / P);
     const int64_t gx = (g.nl + TW - 1) / TW;
     const int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
     int64_t gy = target / gx;
@@ -300,7 +300,7 @@ struct SweepLaunch<float, 2, C> {
     if (gy > g.rows) gy = g.rows;
     const int RB = (int)((g.rows + gy - 1) / gy);
     gy = (g.rows + RB - 1) / RB;
-    k_sweep<C, TW, P><<<dim3((unsigned)gx, (unsigned)gy, 1), TW / P, smem, s>>>(g, a, RB);
+    k_sweep<C, TW, P, DP><<<dim3((unsigned)gx, (unsigned)gy, 1), TW / P, smem, s>>>(g, a, RB);
   }
   // narrow rows get narrow tiles, so that no CTA carries idle threads
   static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
@@ -635,18 +635,17 @@ OPYX_D void load_inst(const BatchInst* src, BatchInst* dst) {
   for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
 }
 
-template <int C, int TW, int P = sweep_p(C)>
+template <int C, int TW, int P = sweep_p(C), int DP = sweep_depth(C)>
 __global__ void __launch_bounds__(TW / P, sweep_min_blocks(TW, P))
 k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
               int nitems, int flip) {
   extern __shared__ float4 smem4[];
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t mbar[kSweepMaxBars];
   __shared__ __align__(16) BatchInst cur;
   float* sm = reinterpret_cast<float*>(smem4);
   const bool lead = threadIdx.x == 0;
   if (lead) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int i = 0; i < kSweepMaxBars; ++i) mbar_init(&mbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -662,7 +661,7 @@ k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__
     }
     if (cur.a.info->done != 0.0) continue;   // uniform: read by every thread alike
     const Args<float> a = flip ? swapped(cur.a) : cur.a;
-    if (!sweep_rows<C, TW, P>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW, P, DP>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();
 }
@@ -781,13 +780,13 @@ static int batch_check(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
 template <int C, int TW>
 static int batch_launch_sweep(const BatchInst* insts, const BatchItem* items, int nitems,
                               int flip, cudaStream_t s) {
-  constexpr int smem = SweepSmem<C, TW>::bytes;
-  constexpr int P = sweep_p(C);
+  constexpr int P = sweep_p(C), DP = sweep_depth(C);
+  constexpr int smem = SweepSmem<C, TW, DP>::bytes;
   static int per_sm = -1;
-  if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep_batch<C, TW, P>, smem, TW / P);
+  if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep_batch<C, TW, P, DP>, smem, TW / P);
   int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
   if (grid > nitems) grid = nitems;
-  k_sweep_batch<C, TW, P><<<(unsigned)grid, TW / P, smem, s>>>(insts, items, nitems, flip);
+  k_sweep_batch<C, TW, P, DP><<<(unsigned)grid, TW / P, smem, s>>>(insts, items, nitems, flip);
   return check_launch();
 }
 

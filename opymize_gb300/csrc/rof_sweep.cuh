@@ -34,12 +34,21 @@
 namespace opyx {
 namespace rof {
 
-template <int C, int TW = kPipeTW>
+// Rows of prefetch (DP): the bulk load of row r + DP is issued when row r
+// is computed.  One channel's row steps are short, so two rows keep DRAM
+// latency hidden; three or four channels keep one (their rings would cost an
+// SM one of its three CTAs).
+constexpr int sweep_depth(int C) { return C <= 2 ? 2 : 1; }
+constexpr int kSweepMaxBars = 3;   // mbarriers per CTA: DP + 1 stages in flight
+
+template <int C, int TW = kPipeTW, int DP = 1>
 struct SweepSmem {
   static constexpr int M = 2 * C;
   static constexpr int X4 = (TW + 4) * C;   // right halo
   static constexpr int Y44 = (TW + 8) * M;  // 4-pixel halo on both sides
-  static constexpr int bytes = 4 * (3 * Y44 + 2 * X4 + 2 * X4 + 2 * X4);
+  static constexpr int NY = DP + 2;         // y rows r-1 .. r+DP
+  static constexpr int NX = DP + 1;         // x, f rows r .. r+DP
+  static constexpr int bytes = 4 * (NY * Y44 + NX * X4 + NX * X4 + 2 * X4);
 };
 
 // Pixels per thread of the sweep: 2 (256 threads per 512-pixel tile), twice
@@ -230,15 +239,15 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
 // sweep, shared by the single-instance and the batched kernels.  `st` counts
 // the stages this CTA has issued on its two mbarriers.  Returns false if a
 // copy did not arrive within the wait bound (info->fault is then set).
-template <int C, int TW, int P>
+template <int C, int TW, int P, int DP>
 OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
                        int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
-  using S = SweepSmem<C, TW>;
-  constexpr int D = 2, M = D * C, NT = TW / P;
-  float* ys = sm;                          // 3 x Y44: row q in slot (q - r0 + 1) % 3
-  float* xs = ys + 3 * S::Y44;             // 2 x X4 : x_k, then x_{k+1}
-  float* fs = xs + 2 * S::X4;              // 2 x X4
-  float* bs = fs + 2 * S::X4;              // 2 x X4 : xbar rows, slot (q - r0) & 1
+  using S = SweepSmem<C, TW, DP>;
+  constexpr int D = 2, M = D * C, NT = TW / P, NB = DP + 1;
+  float* ys = sm;                          // NY x Y44: row q in slot (q - r0 + 1) % NY
+  float* xs = ys + S::NY * S::Y44;         // NX x X4 : x_k, then x_{k+1}; row q in (q - r0) % NX
+  float* fs = xs + S::NX * S::X4;          // NX x X4
+  float* bs = fs + S::NX * S::X4;          // 2 x X4 : xbar rows, slot (q - r0) & 1
   const int lp0 = threadIdx.x * P;
   const bool lead = threadIdx.x == 0;        // issues the bulk copies
   const bool halo = threadIdx.x == NT - 1;   // also computes xbar at pixel TW
@@ -247,45 +256,54 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
   const float sig_c = (float)a.sigma;
   const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
   const int64_t rl = r1 < g.rows ? r1 : r1 - 1;   // last row whose pass A runs here
+  // stage of row q (r0 <= q <= rl) is base + (q - r0), on mbar[stage % NB]
+  const unsigned base = st;
   if (lead) {
     bulk_wait_read_all();
     fence_proxy_async();
-    issue_stage<C, TW>(g, a, q_beg, &mbar[st & 1], ys, r0 - 1, ys + S::Y44, r0, xs, fs, r0);
+    for (int64_t q = r0; q <= rl && q < r0 + DP; ++q) {
+      const unsigned sq = base + (unsigned)(q - r0);
+      const int kq = (int)(q - r0);
+      issue_stage<C, TW>(g, a, q_beg, &mbar[sq % NB], q == r0 ? ys : nullptr, r0 - 1,
+                         ys + ((kq + 1) % S::NY) * S::Y44, q, xs + (kq % S::NX) * S::X4,
+                         fs + (kq % S::NX) * S::X4, q);
+    }
   }
-  unsigned cur = st++;
   for (int64_t r = r0; r <= r1; ++r) {
     const int k = (int)(r - r0);
     const bool run_a = r <= rl;
-    const bool more = r + 1 <= rl;
-    unsigned nxt = cur;
-    if (more) {
-      if (lead) {
-        bulk_wait_read_all();   // stores still reading the slots about to be refilled
-        fence_proxy_async();
-        issue_stage<C, TW>(g, a, q_beg, &mbar[st & 1], nullptr, 0, ys + ((k + 2) % 3) * S::Y44,
-                       r + 1, xs + ((k + 1) & 1) * S::X4, fs + ((k + 1) & 1) * S::X4, r + 1);
-      }
-      nxt = st++;
+    const int64_t rn = r + DP;                 // row whose copies start now
+    if (rn <= rl && lead) {
+      bulk_wait_read_all();   // stores still reading the slots about to be refilled
+      fence_proxy_async();
+      const int kn = (int)(rn - r0);
+      issue_stage<C, TW>(g, a, q_beg, &mbar[(base + (unsigned)kn) % NB], nullptr, 0,
+                         ys + ((kn + 1) % S::NY) * S::Y44, rn, xs + (kn % S::NX) * S::X4,
+                         fs + (kn % S::NX) * S::X4, rn);
     }
+    const unsigned cur = base + (unsigned)k;
     bool ok = true;
-    if (run_a) ok = mbar_wait(&mbar[cur & 1], (cur >> 1) & 1u);
+    if (run_a) ok = mbar_wait(&mbar[cur % NB], (cur / NB) & 1u);
     if (__syncthreads_or(!ok)) {
       // a copy did not arrive within the bound: flag it, give the copies
       // in flight a bounded chance to land, and leave
       if (lead) {
         a.info->fault = 1.0;
         a.info->done = 1.0;
-        if (more) mbar_wait(&mbar[nxt & 1], (nxt >> 1) & 1u);
+        for (int64_t q = r; q <= rl && q <= rn; ++q) {   // every stage still in flight
+          const unsigned sq = base + (unsigned)(q - r0);
+          mbar_wait(&mbar[sq % NB], (sq / NB) & 1u);
+        }
         bulk_wait_all();
       }
       return false;
     }
-    const float* yc = ys + ((k + 1) % 3) * S::Y44;    // y_k row r
-    float* yu = ys + (k % 3) * S::Y44;                // y_k row r - 1
-    float* xv = xs + (k & 1) * S::X4;
-    const float* fv = fs + (k & 1) * S::X4;
-    float* bc = bs + (k & 1) * S::X4;                 // xbar row r
-    const float* bu = bs + ((k + 1) & 1) * S::X4;     // xbar row r - 1
+    const float* yc = ys + ((k + 1) % S::NY) * S::Y44;    // y_k row r
+    float* yu = ys + (k % S::NY) * S::Y44;                // y_k row r - 1
+    float* xv = xs + (k % S::NX) * S::X4;
+    const float* fv = fs + (k % S::NX) * S::X4;
+    float* bc = bs + (k & 1) * S::X4;                     // xbar row r
+    const float* bu = bs + ((k + 1) & 1) * S::X4;         // xbar row r - 1
     // ---- pass A, row r (and xbar at the first pixel past the tile)
     if (run_a) {
       float qx[P * C], qb[P * C];
@@ -350,30 +368,29 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       if (lead) store_span<M, 4, TW>(a.y2, yu, g, rb, q_beg);
     }
     __syncthreads();
-    cur = nxt;
   }
-    return true;
+  st = base + (unsigned)(rl - r0 + 1);
+  return true;
 }
 
-template <int C, int TW = kPipeTW, int P = kSweepP>
+template <int C, int TW = kPipeTW, int P = kSweepP, int DP = 1>
 __global__ void __launch_bounds__(TW / P, sweep_min_blocks(TW, P))
 k_sweep(Geo<float> g, Args<float> a, int RB) {
   if (stopped(a)) return;
   extern __shared__ float4 smem4[];
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t mbar[kSweepMaxBars];
   float* sm = reinterpret_cast<float*>(smem4);
   const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const bool lead = threadIdx.x == 0;
   if (lead) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int i = 0; i < kSweepMaxBars; ++i) mbar_init(&mbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  unsigned st = 0;   // stages issued so far; stage s uses mbar[s & 1], parity (s >> 1) & 1
+  unsigned st = 0;   // stages issued so far; stage s uses mbar[s % (DP+1)]
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    if (!sweep_rows<C, TW, P>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW, P, DP>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }
