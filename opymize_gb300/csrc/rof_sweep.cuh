@@ -106,7 +106,10 @@ OPYX_D void sts(float* __restrict__ p, const float (&d)[NF]) {
 
 // Pass A of NP consecutive pixels from local pixel lp (0..TW) of row r:
 // x_{k+1} (into qx) and xbar (into qb), as k_passA_p.
-template <int C, int NP>
+// WARP: called by all 32 lanes of a warp on consecutive pixel groups (the
+// left neighbour's y comes from the lane below by a shuffle; lane 0 reads
+// shared memory), else by a single thread (the halo pixel).
+template <int C, int NP, bool WARP = true>
 OPYX_D void sweep_a(const Geo<float>& g, const Args<float>& a, const PrimalCoefs<float, C>& pc,
                     bool pre, const float* yc, const float* yu, const float* xv, const float* fv,
                     int64_t r, int64_t q_beg, int lp, float (&qx)[NP * C], float (&qb)[NP * C]) {
@@ -118,8 +121,17 @@ OPYX_D void sweep_a(const Geo<float>& g, const Args<float>& a, const PrimalCoefs
   lds(qu, yu + (lp + 4) * M);
   lds(qx, xv + lp * C);
   lds(qf, fv + lp * C);
+  if (WARP) {
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int k2 = 0; k2 < C; ++k2) yl[k2] = yc[(lp + 3) * M + (D - 1) * C + k2];
+    for (int k2 = 0; k2 < C; ++k2) {
+      const float up = __shfl_up_sync(0xffffffffu, qy[(NP - 1) * M + (D - 1) * C + k2], 1);
+      yl[k2] = lane ? up : yc[(lp + 3) * M + (D - 1) * C + k2];
+    }
+  } else {
+#pragma unroll
+    for (int k2 = 0; k2 < C; ++k2) yl[k2] = yc[(lp + 3) * M + (D - 1) * C + k2];
+  }
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
     const int64_t q = qt + p;
@@ -311,7 +323,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       float hb[C];
       if (halo) {
         float hx[C];
-        sweep_a<C, 1>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, TW, hx, hb);
+        sweep_a<C, 1, false>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, TW, hx, hb);
       }
       __syncthreads();   // every thread has read the x_k values it needs
       sts(xv + lp0 * C, qx);
@@ -331,8 +343,16 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       lds(qx, bu + lp0 * C);
       lds(qn, bc + lp0 * C);
       lds(qy, yu + (lp0 + 4) * M);
+      {
+        // right neighbour's xbar from the lane above; lane 31 reads shared
+        // memory (for the CTA's last thread: the halo pixel)
+        const int lane = threadIdx.x & 31;
 #pragma unroll
-      for (int k2 = 0; k2 < C; ++k2) xr[k2] = bu[(lp0 + P) * C + k2];
+        for (int k2 = 0; k2 < C; ++k2) {
+          const float dn = __shfl_down_sync(0xffffffffu, qx[k2], 1);
+          xr[k2] = lane < 31 ? dn : bu[(lp0 + P) * C + k2];
+        }
+      }
 #pragma unroll
       for (int p = 0; p < P; ++p) {
         const int64_t q = q_beg + lp0 + p;
