@@ -666,7 +666,11 @@ k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__
   if (lead) bulk_wait_all();
 }
 
-// Per-item partial sums of the gap (as k_gap): {G, |Ax|, G*, |y|^2, max(|y| - lbd)}.
+// Per-item partial sums of the gap (as k_gap_p): {G, |Ax|, G*, |y|^2,
+// max(|y| - lbd)}.  A thread owns one quad (4 pixels along the row) of a run
+// of consecutive rows of the item, carries x of the next row and y of the
+// current row into the following row, and accumulates in FP32 over its
+// pixels; FP64 across the block.
 template <int C>
 __global__ void __launch_bounds__(256)
 k_gap_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
@@ -685,47 +689,76 @@ k_gap_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ i
     }
     const Geo<float>& g = cur.g;
     const Args<float>& a = cur.a;
-    double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
-    if (a.info->done == 0.0) {
-      const int64_t qe = item.q_end;
-      const int64_t w = qe - item.q_beg;
-      const int64_t npx = w * (item.r1 - item.r0);
-      for (int64_t t = threadIdx.x; t < npx; t += blockDim.x) {
-        const int64_t r = item.r0 + t / w, q = item.q_beg + t % w;
-        const int64_t i = r * g.nl + q;
-        int64_t c[3];
-        coords<float, D>(g, r, q, c);
-        float ax[M], div[C];
-        grad_at<float, D, C>(g, a.x, i, c, ax);
-        div_at<float, D, C>(g, a.y, i, c, div);
-        const bool on = !a.mask || a.mask[i];
-        if (on) {
-          float pg = 0.f, ps = 0.f;
+    float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;
+    const int nq = (int)((item.q_end - item.q_beg) >> 2);     // quads per row, <= 128
+    const int rstep = (int)blockDim.x / nq;                     // row runs per block
+    const int tq = (int)threadIdx.x % nq, tr = (int)threadIdx.x / nq;
+    const int nr = item.r1 - item.r0;
+    const int rpt = (nr + rstep - 1) / rstep;
+    const int64_t rb = item.r0 + (int64_t)tr * rpt;
+    const int64_t re = rb + rpt < item.r1 ? rb + rpt : item.r1;
+    if (a.info->done == 0.0 && tr < rstep && rb < re) {
+      const int64_t q0 = item.q_beg + 4 * tq;
+      const int64_t nl = g.nl, nrow = g.n[0];
+      const bool has_r = q0 + 4 < nl, has_l = q0 > 0;
+      float qx[4 * C], qn[4 * C], qf[4 * C], qy[4 * M], qu[4 * M], xr[C], yl[C];
+      ldv(qx, a.x + (rb * nl + q0) * C);
+      if (rb > 0) ldv(qu, a.y + ((rb - 1) * nl + q0) * M);
+      else zero(qu);
+      for (int64_t r = rb; r < re; ++r) {
+        const int64_t i0 = r * nl + q0;
+        const bool has_up = r > 0, has_dn = r < nrow - 1;
+        if (has_dn) ldv(qn, a.x + (i0 + nl) * C);
+        else zero(qn);
+        ldv(qy, a.y + i0 * M);
+        ldv(qf, a.f + i0 * C);
 #pragma unroll
-          for (int k = 0; k < C; ++k) {
-            const float fk = a.f[i * C + k];
-            const float d = a.x[i * C + k] - fk;
-            pg += g.vol[k] * d * d;
-            ps += div[k] * div[k] * g.half_rvol[k] - fk * div[k];
+        for (int k2 = 0; k2 < C; ++k2) {
+          xr[k2] = has_r ? a.x[(i0 + 4) * C + k2] : 0.f;
+          yl[k2] = has_l ? a.y[(i0 - 1) * M + (D - 1) * C + k2] : 0.f;
+        }
+        unsigned mk = 0xffffffffu;
+        if (a.mask) mk = *reinterpret_cast<const unsigned*>(a.mask + i0);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          const int64_t q = q0 + p;
+          const bool on = (mk >> (8 * p)) & 0xffu;
+          const bool inx = q < nl - 1;
+          float n2 = 0.f, y2 = 0.f;
+#pragma unroll
+          for (int k2 = 0; k2 < C; ++k2) {
+            const float xk = qx[p * C + k2], fk = qf[p * C + k2];
+            float s = 0.f;
+            const float ihl = g.invh[D - 1], ihr = g.invh[D - 2];
+            if (inx) s -= qy[p * M + (D - 1) * C + k2] * ihl;
+            if (q > 0) s += (p > 0 ? qy[(p - 1) * M + (D - 1) * C + k2] : yl[k2]) * ihl;
+            if (has_dn) s -= qy[p * M + (D - 2) * C + k2] * ihr;
+            if (has_up) s += qu[p * M + (D - 2) * C + k2] * ihr;
+            const float ak = g.w[k2] * s;
+            if (on) {
+              const float d = xk - fk;
+              pG += g.vol[k2] * d * d;
+              pGs += ak * ak * g.half_rvol[k2] - fk * ak;
+            }
+            const float nb = p < 3 ? qx[(p + 1) * C + k2] : xr[k2];
+            const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
+            const float gr = has_dn ? g.coef[D - 2][k2] * (qn[p * C + k2] - xk) : 0.f;
+            n2 += gl * gl + gr * gr;
           }
-          sG += 0.5 * (double)pg;
-          sGs += (double)ps;
-        }
-        float n2 = 0.f, y2 = 0.f;
 #pragma unroll
-        for (int j = 0; j < M; ++j) {
-          n2 += ax[j] * ax[j];
-          const float yj = a.y[i * M + j];
-          y2 += yj * yj;
+          for (int j = 0; j < M; ++j) y2 += qy[p * M + j] * qy[p * M + j];
+          const float nrm = sqrtf(n2);
+          pF += g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
+          pFs += y2;
+          pinf = fmaxf(pinf, sqrtf(y2) - g.lbd);
         }
-        const float nrm = sqrtf(n2);
-        const float fv = g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
-        sF += (double)fv;
-        sFs += (double)y2;
-        inf = fmax(inf, (double)(sqrtf(y2) - g.lbd));
+#pragma unroll
+        for (int j = 0; j < 4 * C; ++j) qx[j] = qn[j];
+#pragma unroll
+        for (int j = 0; j < 4 * M; ++j) qu[j] = qy[j];
       }
     }
-    double v[5] = {sG, sF, sGs, sFs, inf};
+    double v[5] = {0.5 * (double)pG, (double)pF, (double)pGs, (double)pFs, (double)pinf};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
@@ -735,7 +768,7 @@ k_gap_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ i
     __syncthreads();
     if (threadIdx.x < 5) {
       const int k = threadIdx.x;
-      double r = k == 4 ? 0.0 : 0.0;
+      double r = k == 4 ? -INFINITY : 0.0;
       for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2)
         r = k == 4 ? fmax(r, red[k][w2]) : r + red[k][w2];
       partials[(size_t)it * 5 + k] = r;
