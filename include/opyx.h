@@ -412,10 +412,16 @@ int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int whic
  *   term_mode, `done`, `fault` as for single solves).
  * opyx_rof_batch_describe fills, ON THE HOST, a descriptor of
  *   opyx_rof_batch_desc_bytes(ninst, nitems) bytes: per instance its
- *   coefficients and pointers, and work items (rows_per_item rows x 512
- *   pixels) for the instances with active[i] != 0 (all if active is NULL);
+ *   coefficients and pointers, and work items (rows_per_item rows x 128,
+ *   256 or 512 pixels: the narrowest tile width that holds the instance's
+ *   rows) for the instances with active[i] != 0 (all if active is NULL);
  *   the caller copies it to device memory and passes both copies below (the
  *   host copy for the launch shapes, the device copy to the kernels).
+ *   *nitems receives the work item count; with host_desc NULL and
+ *   host_bytes 0 (or any buffer too small) the call returns
+ *   OPYX_ERR_WORKSPACE after setting it, so a first call sizes the buffer.
+ *   An item's tile spans [q_beg, q_end) of its rows; the sweep stores
+ *   nothing past q_end.
  * opyx_rof_batch_init writes every instance's step state and clears its info.
  * opyx_rof_batch_iterate runs `iters` (even) iterations of the active items.
  * opyx_rof_batch_gap evaluates the gap of every instance with items, using

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_PKG, "libopyx.so")
 
 OPYX_OK = 0
 OPYX_ERR_LAUNCH = 2
+OPYX_ERR_WORKSPACE = 4
 OPYX_F32, OPYX_F64 = 0, 1
 SCHEME = {"forward": 0, "centered": 1}
 BC = {"neumann": 0, "curvature": 1, "second-order": 2}

@@ -603,7 +603,15 @@ constexpr size_t kBatchRecord = 512;   // [0, 256) step state, [256, 512) info
 constexpr int kBatchClasses = 3;
 constexpr int kBatchTW[kBatchClasses] = {128, 256, 512};
 
-static int batch_class(int64_t nl) { return nl <= 128 ? 0 : nl <= 256 ? 1 : 2; }
+// Column tiles of an instance with rows of nl pixels: the narrowest class
+// whose width holds the row (else 512), tiles of the class width, the last
+// one narrower.  (Equal-width narrower tiles fill the CTAs better but cost
+// the gap evaluation more than the sweep gains on mixed-size batches.)
+static int batch_tiles(int64_t nl, int64_t* tw) {
+  const int c = nl <= kBatchTW[0] ? 0 : nl <= kBatchTW[1] ? 1 : 2;
+  *tw = kBatchTW[c];
+  return c;
+}
 
 struct BatchHeader {
   int32_t ninst, nitems, nchannels, pad;
@@ -651,8 +659,19 @@ k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__
   __syncthreads();
   unsigned st = 0;
   int loaded = -1;
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+  // a contiguous share of the item list per CTA; runs of vertically adjacent
+  // items of one tile column are swept as one range of rows (one prologue,
+  // no halo row between them)
+  const int64_t lo = (int64_t)nitems * blockIdx.x / gridDim.x;
+  const int64_t hi = (int64_t)nitems * (blockIdx.x + 1) / gridDim.x;
+  for (int64_t it = lo; it < hi;) {
     const BatchItem item = items[it];
+    int32_t r1 = item.r1;
+    for (++it; it < hi; ++it) {
+      const BatchItem nx = items[it];
+      if (nx.inst != item.inst || nx.q_beg != item.q_beg || nx.r0 != r1) break;
+      r1 = nx.r1;
+    }
     if (item.inst != loaded) {
       __syncthreads();   // nobody still reads the previous instance
       load_inst(&insts[item.inst], &cur);
@@ -661,7 +680,8 @@ k_sweep_batch(const BatchInst* __restrict__ insts, const BatchItem* __restrict__
     }
     if (cur.a.info->done != 0.0) continue;   // uniform: read by every thread alike
     const Args<float> a = flip ? swapped(cur.a) : cur.a;
-    if (!sweep_rows<C, TW, P, DP>(cur.g, a, item.q_beg, item.r0, item.r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW, P, DP>(cur.g, a, item.q_beg, item.q_end, item.r0, r1, mbar, st, sm))
+      return;
   }
   if (lead) bulk_wait_all();
 }
@@ -850,7 +870,8 @@ size_t opyx_rof_batch_desc_bytes(int ninst, int nitems) {
 int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffers* bufs,
                             int ninst, void* records, const uint8_t* active, int rows_per_item,
                             void* host_desc, size_t host_bytes, int* nitems_out) {
-  if (!probs || !bufs || ninst < 1 || !records || rows_per_item < 1 || !host_desc || !nitems_out)
+  if (!probs || !bufs || ninst < 1 || !records || rows_per_item < 1 || (!host_desc && host_bytes) ||
+      !nitems_out)
     return OPYX_ERR_ARG;
   if (((uintptr_t)records) & 255) return OPYX_ERR_WORKSPACE;
   const int C = probs[0].nchannels;
@@ -862,12 +883,14 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
     if (st) return st;
     if (probs[i].nchannels != C) return OPYX_ERR_ARG;
     if (active && !active[i]) continue;
-    const int64_t tw = kBatchTW[batch_class(probs[i].dims[1])];
+    int64_t tw;
+    batch_tiles(probs[i].dims[1], &tw);
     const int64_t gx = (probs[i].dims[1] + tw - 1) / tw;
     const int64_t gy = (probs[i].dims[0] + rows_per_item - 1) / rows_per_item;
     nitems += gx * gy;
   }
   if (nitems > INT32_MAX) return OPYX_ERR_UNSUPPORTED;
+  *nitems_out = (int)nitems;   // also on OPYX_ERR_WORKSPACE: the size to allocate
   if (host_bytes < opyx_rof_batch_desc_bytes(ninst, (int)nitems)) return OPYX_ERR_WORKSPACE;
   char* base = (char*)host_desc;
   BatchHeader* h = (BatchHeader*)base;
@@ -900,11 +923,14 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
     h->class_beg[c] = k;
     for (int i = 0; i < ninst; ++i) {
       const opyx_rof_problem* p = &probs[i];
-      if ((active && !active[i]) || batch_class(p->dims[1]) != c) continue;
-      const int64_t rows = p->dims[0], nl = p->dims[1], tw = kBatchTW[c];
+      int64_t tw;
+      if ((active && !active[i]) || batch_tiles(p->dims[1], &tw) != c) continue;
+      const int64_t rows = p->dims[0], nl = p->dims[1];
       insts[i].item_beg = k;
-      for (int64_t r0 = 0; r0 < rows; r0 += rows_per_item)
-        for (int64_t q = 0; q < nl; q += tw) {
+      // tile columns outer: vertically adjacent items are consecutive, so a
+      // CTA whose share holds several sweeps them as one run of rows
+      for (int64_t q = 0; q < nl; q += tw)
+        for (int64_t r0 = 0; r0 < rows; r0 += rows_per_item) {
           BatchItem& it = items[k++];
           it.inst = i;
           it.r0 = (int32_t)r0;

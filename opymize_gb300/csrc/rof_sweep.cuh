@@ -236,24 +236,28 @@ OPYX_D void issue_stage(const Geo<float>& g, const Args<float>& a, int64_t q_beg
   if (bf) bulk_load(fsl + of * C, a.f + sf * C, bf, m);
 }
 
-// Thread 0: store the TW pixels of a slot (after HL halo pixels) to row r.
+// Thread 0: store the pixels [q_beg, min(q_beg + TW, q_end)) of a slot
+// (after HL halo pixels) to row r.
 template <int E, int HL, int TW>
 OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64_t r,
-                       int64_t q_beg) {
-  const int64_t hi = q_beg + TW < g.nl ? q_beg + TW : g.nl;
+                       int64_t q_beg, int64_t q_end) {
+  const int64_t lim = q_end < g.nl ? q_end : g.nl;
+  const int64_t hi = q_beg + TW < lim ? q_beg + TW : lim;
   if (hi <= q_beg) return;
   fence_proxy_async();   // the threads' shared-memory writes, before the copy reads them
   bulk_store(arr + (r * g.nl + q_beg) * E, slot + HL * E, (unsigned)((hi - q_beg) * E * 4));
   bulk_commit();
 }
 
-// One run of rows [r0, r1) of the column tile at q_beg: the body of the
-// sweep, shared by the single-instance and the batched kernels.  `st` counts
-// the stages this CTA has issued on its two mbarriers.  Returns false if a
-// copy did not arrive within the wait bound (info->fault is then set).
+// One run of rows [r0, r1) of the column tile [q_beg, q_end) (at most TW
+// pixels): the body of the sweep, shared by the single-instance and the
+// batched kernels.  Pixels of the slot past q_end are computed from the
+// loaded rows but not stored (their own tile stores them).  `st` counts the
+// stages this CTA has issued on its mbarriers.  Returns false if a copy did
+// not arrive within the wait bound (info->fault is then set).
 template <int C, int TW, int P, int DP>
-OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
-                       int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
+OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t q_end,
+                       int64_t r0, int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
   using S = SweepSmem<C, TW, DP>;
   constexpr int D = 2, M = D * C, NT = TW / P, NB = DP + 1;
   float* ys = sm;                          // NY x Y44: row q in slot (q - r0 + 1) % NY
@@ -334,7 +338,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       }
     }
     __syncthreads();
-    if (lead && r < r1) store_span<C, 0, TW>(a.x2, xv, g, r, q_beg);
+    if (lead && r < r1) store_span<C, 0, TW>(a.x2, xv, g, r, q_beg, q_end);
     // ---- pass B, row r - 1 (as k_passB_p), in place in its y slot
     if (r > r0) {
       const int64_t rb = r - 1;
@@ -385,7 +389,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
       }
       sts(yu + (lp0 + 4) * M, qy);
       __syncthreads();
-      if (lead) store_span<M, 4, TW>(a.y2, yu, g, rb, q_beg);
+      if (lead) store_span<M, 4, TW>(a.y2, yu, g, rb, q_beg, q_end);
     }
     __syncthreads();
   }
@@ -410,7 +414,7 @@ k_sweep(Geo<float> g, Args<float> a, int RB) {
   unsigned st = 0;   // stages issued so far; stage s uses mbar[s % (DP+1)]
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    if (!sweep_rows<C, TW, P, DP>(g, a, q_beg, r0, r1, mbar, st, sm)) return;
+    if (!sweep_rows<C, TW, P, DP>(g, a, q_beg, g.nl, r0, r1, mbar, st, sm)) return;
   }
   if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }

@@ -83,20 +83,19 @@ class BatchROF(object):
     def _describe(self, active, rows):
         lib = _lib.load()
         act = np.ascontiguousarray(active, dtype=np.uint8)
-        nmax = 0
-        for i in range(self.n):
-            if act[i]:
-                H, W, _ = self.dims[i]
-                tw = 128 if W <= 128 else 256 if W <= 256 else 512
-                nmax += -(-H // rows) * -(-W // tw)
-        nbytes = lib.opyx_rof_batch_desc_bytes(self.n, nmax)
-        host = np.zeros(nbytes, dtype=np.uint8)
         nitems = _lib.C.c_int(0)
-        widths = [self.dims[i][1] for i in range(self.n) if act[i]]
-        self._classes = len({0 if w <= 128 else 1 if w <= 256 else 2 for w in widths})
+        # a first call without a buffer returns the item count to size it
+        st = lib.opyx_rof_batch_describe(self.problems, self.buffers, self.n, self.records.ptr,
+                                         act.ctypes.data, int(rows), None, 0, _lib.C.byref(nitems))
+        if st not in (_lib.OPYX_OK, _lib.OPYX_ERR_WORKSPACE):
+            raise _lib.OpyxError("opyx_rof_batch_describe", st, _lib.status_string(st))
+        nbytes = lib.opyx_rof_batch_desc_bytes(self.n, nitems.value)
+        host = np.zeros(nbytes, dtype=np.uint8)
         _lib.call("opyx_rof_batch_describe", self.problems, self.buffers, self.n,
                   self.records.ptr, act.ctypes.data, int(rows), host.ctypes.data, nbytes,
                   _lib.C.byref(nitems))
+        cb = host[16:32].view(np.int32)              # the header's class_beg[0..3]
+        self._classes = int(np.count_nonzero(np.diff(cb)))
         t = torch()
         dev = t.from_numpy(host).to("cuda")
         part = DeviceArray.empty((max(1, nitems.value) * 5,), np.float64)
