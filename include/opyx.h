@@ -460,6 +460,68 @@ int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void* y, const 
  * (FP64 device reductions; pdhg.py:23-44, :287-305). */
 int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);
 
+
+/* ---- Learned warm start: U-Net kernels (BF16 tensor cores, FP32 accumulation) ----
+ * Activations are NHWC bf16 with `stride` channels per pixel; a layer reads
+ * or writes the channel slice [offset, offset + channels).  3x3 convolutions
+ * are implicit GEMMs on the tcgen05 tensor cores (TMEM accumulators, TMA
+ * operand copies): 128-pixel tiles of one or more whole rows, so
+ * min(width, 128) must divide 128 and the width, and 128 / min(width, 128)
+ * the height.  Weights are bf16 [9][out_channels][in_channels] (tap = 3 *
+ * (dy + 1) + (dx + 1)).  No counterpart in the reference (its solvers start
+ * from zero or from `continue_at`, opymize/solvers/pdhg.py:229-255). */
+enum { OPYX_CONV_GELU = 0, OPYX_CONV_F32 = 1, OPYX_CONV_BF16 = 2 };
+
+typedef struct {
+  int32_t batch, height, width;
+  int32_t in_channels, in_stride, in_offset;    /* in_channels a multiple of 32 */
+  int32_t out_channels, out_stride, out_offset; /* out_channels 32, 64, 128 or 256 */
+  int32_t epilogue;   /* GELU: y = gelu(acc + bias) bf16 and z = acc + bias (bf16, dense,
+                         if z != NULL); F32: y (+)= acc + bias as fp32; BF16: y = acc + bias */
+  int32_t accumulate; /* F32 epilogue: add into y */
+  const void* x;      /* bf16 activations */
+  const void* w;      /* bf16 weights */
+  const float* bias;  /* [out_channels] or NULL */
+  void* y;
+  void* z;
+} opyx_conv3x3_desc;
+
+int opyx_conv3x3(const opyx_conv3x3_desc* d, void* stream);
+/* dw[tap][co][ci] (+)= sum_p x[p + offset(tap), ci] * dy[p, co] (fp32), dy
+ * dense bf16 [batch, height, width, out_channels] (32, 64 or 128). */
+size_t opyx_conv3x3_wgrad_workspace(const opyx_conv3x3_desc* d);
+int opyx_conv3x3_wgrad(const opyx_conv3x3_desc* d, const void* dy, float* dw, int accumulate,
+                       void* ws, size_t ws_bytes, void* stream);
+/* Sticky flag set by a network kernel that gave up a bounded wait. */
+int opyx_net_fault(unsigned* out);
+/* dz = da * gelu'(z) (bf16, dense), dbias (+)= column sums of dz. */
+size_t opyx_gelu_bwd_workspace(int64_t npix, int C);
+int opyx_gelu_bwd(int64_t npix, int C, const float* da, int da_stride, int da_off, const void* z,
+                  void* dz, float* dbias, int accumulate, void* ws, size_t ws_bytes, void* stream);
+int opyx_pool2(int B, int H, int W, int C, const void* x, int xs, int xo, void* y, void* stream);
+int opyx_pool2_bwd(int B, int H, int W, int C, const float* dy, float* dx, int dxs, int dxo,
+                   int accumulate, void* stream);
+int opyx_up2(int B, int h, int w, int C, const void* x, void* y, int ys, int yo, void* stream);
+int opyx_up2_bwd(int B, int h, int w, int C, const float* dy, int dys, int dyo, float* dx,
+                 void* stream);
+/* Input channels: f, lambda * lam_scale (per image), zeros up to 32 (bf16). */
+int opyx_pack_input(int B, int64_t hw, const float* f, const float* lam, double lam_scale, void* x,
+                    void* stream);
+/* 1x1 head to K = 3 outputs (fp32) and its backward. */
+int opyx_head(int64_t npix, int K, const void* a, const float* w, const float* b, float* out,
+              void* stream);
+size_t opyx_head_bwd_workspace(int64_t npix, int K);
+int opyx_head_bwd(int64_t npix, int K, const void* a, const float* w, const float* dout, float* da,
+                  float* dw, float* db, void* ws, size_t ws_bytes, void* stream);
+/* Weighted mean squared error: grad = 2 wk (pred - tgt) / n, per-block loss partials (fp64). */
+int opyx_mse(int64_t n, int K, const float* pred, const float* tgt, const float* wk, float* grad,
+             double* partials, int nparts, void* stream);
+/* Adam step on fp32 weights; wb / wt (optional): bf16 copy, and the
+ * tap-flipped [9][in][out] copy for input-gradient convolutions. */
+int opyx_adam(int64_t n, float* w, const float* g, float* m, float* v, double lr, double b1, double b2,
+              double eps, int step, void* wb, void* wt, int cin, int cout, void* stream);
+int opyx_conv_weights(int cin, int cout, const float* w, void* wb, void* wt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,17 @@ class opyx_rof_info(C.Structure):
 
 ROF_INFO_FIELDS = [n for n, _ in opyx_rof_info._fields_]
 
+OPYX_CONV_GELU, OPYX_CONV_F32, OPYX_CONV_BF16 = 0, 1, 2
+
+
+class opyx_conv3x3_desc(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
+                ("in_channels", C.c_int32), ("in_stride", C.c_int32), ("in_offset", C.c_int32),
+                ("out_channels", C.c_int32), ("out_stride", C.c_int32), ("out_offset", C.c_int32),
+                ("epilogue", C.c_int32), ("accumulate", C.c_int32),
+                ("x", C.c_void_p), ("w", C.c_void_p), ("bias", C.c_void_p),
+                ("y", C.c_void_p), ("z", C.c_void_p)]
+
 
 vp, i32, i64, f64, sz = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_size_t
 P = C.POINTER
@@ -161,6 +172,23 @@ SIGNATURES = {
     "opyx_rof_batch_init": (i32, [vp, vp, vp]),
     "opyx_rof_batch_iterate": (i32, [vp, vp, i32, vp]),
     "opyx_rof_batch_gap": (i32, [vp, vp, vp, vp]),
+    "opyx_conv3x3": (i32, [P(opyx_conv3x3_desc), vp]),
+    "opyx_conv3x3_wgrad_workspace": (sz, [P(opyx_conv3x3_desc)]),
+    "opyx_conv3x3_wgrad": (i32, [P(opyx_conv3x3_desc), vp, vp, i32, vp, sz, vp]),
+    "opyx_net_fault": (i32, [P(C.c_uint)]),
+    "opyx_gelu_bwd_workspace": (sz, [i64, i32]),
+    "opyx_gelu_bwd": (i32, [i64, i32, vp, i32, i32, vp, vp, vp, i32, vp, sz, vp]),
+    "opyx_pool2": (i32, [i32, i32, i32, i32, vp, i32, i32, vp, vp]),
+    "opyx_pool2_bwd": (i32, [i32, i32, i32, i32, vp, vp, i32, i32, i32, vp]),
+    "opyx_up2": (i32, [i32, i32, i32, i32, vp, vp, i32, i32, vp]),
+    "opyx_up2_bwd": (i32, [i32, i32, i32, i32, vp, i32, i32, vp, vp]),
+    "opyx_pack_input": (i32, [i32, i64, vp, vp, f64, vp, vp]),
+    "opyx_head": (i32, [i64, i32, vp, vp, vp, vp, vp]),
+    "opyx_head_bwd_workspace": (sz, [i64, i32]),
+    "opyx_head_bwd": (i32, [i64, i32, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
+    "opyx_mse": (i32, [i64, i32, vp, vp, vp, vp, vp, i32, vp]),
+    "opyx_adam": (i32, [i64, vp, vp, vp, vp, f64, f64, f64, f64, i32, vp, vp, i32, i32, vp]),
+    "opyx_conv_weights": (i32, [i32, i32, vp, vp, vp, vp]),
 }
 
 _lib = None
