@@ -516,6 +516,18 @@ int opyx_head_bwd(int64_t npix, int K, const void* a, const float* w, const floa
 /* Weighted mean squared error: grad = 2 wk (pred - tgt) / n, per-block loss partials (fp64). */
 int opyx_mse(int64_t n, int K, const float* pred, const float* tgt, const float* wk, float* grad,
              double* partials, int nparts, void* stream);
+/* Warm-start loss on head outputs out = (x - f, y / lambda) against targets:
+ * (1/n) sum w_x (o0 - t0)^2 + w_div (lambda div(o12 - t12))^2 + w_u |o12 - t12|^2
+ * + w_pool (4096/n) sum over 8x8 blocks of (block mean of o0 - t0)^2 + (block
+ * mean of lambda div(o12 - t12))^2, with div adjoint to the forward gradient;
+ * writes d loss / d out (grad) and per-block loss partials; scratch holds
+ * B*H*W + B*H*W/32 floats (H, W multiples of 8 when w_pool != 0). */
+int opyx_warm_loss(int B, int H, int W, const float* out, const float* tgt, const float* lam,
+                   double w_x, double w_div, double w_u, double w_pool, float* grad, float* scratch,
+                   double* partials, int nparts, void* stream);
+/* Proposal from head outputs: x0 = f + o0, y0 = lambda * o12 / max(1, |o12|). */
+int opyx_warm_unpack(int B, int64_t hw, const float* f, const float* lam, const float* out, float* x0,
+                     float* y0, void* stream);
 /* Adam step on fp32 weights; wb / wt (optional): bf16 copy, and the
  * tap-flipped [9][in][out] copy for input-gradient convolutions. */
 int opyx_adam(int64_t n, float* w, const float* g, float* m, float* v, double lr, double b1, double b2,

@@ -187,6 +187,8 @@ SIGNATURES = {
     "opyx_head_bwd_workspace": (sz, [i64, i32]),
     "opyx_head_bwd": (i32, [i64, i32, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "opyx_mse": (i32, [i64, i32, vp, vp, vp, vp, vp, i32, vp]),
+    "opyx_warm_loss": (i32, [i32, i32, i32, vp, vp, vp, f64, f64, f64, f64, vp, vp, vp, i32, vp]),
+    "opyx_warm_unpack": (i32, [i32, i64, vp, vp, vp, vp, vp, vp]),
     "opyx_adam": (i32, [i64, vp, vp, vp, vp, f64, f64, f64, f64, i32, vp, vp, i32, i32, vp]),
     "opyx_conv_weights": (i32, [i32, i32, vp, vp, vp, vp]),
 }

@@ -610,6 +610,134 @@ __global__ void k_mse(int64_t n, int K, const float* __restrict__ pred, const fl
   }
 }
 
+// Warm-start loss.  Head outputs per pixel: o0 = x - f, (o1, o2) = y / lambda
+// (components along rows and columns).  With e = o[1:3] - t[1:3] and the
+// divergence d = div(e) adjoint to the forward gradient (div v =
+// sum_t v_t[i] [c_t < n_t - 1] - v_t[i - s_t] [c_t > 0]), the loss is
+//   (1/n) sum_i  w_x (o0 - t0)^2 + w_div (lambda d)^2 + w_u |e|^2 :
+// the dual enters through lambda div(y / lambda) = div y, which is what the
+// duality gap sees (at the optimum x - f = div y), while y itself is only
+// determined up to divergence-free fields where x is flat.
+// A fourth term weights the low frequencies, where PDHG converges slowly:
+// with R = 8x8 block means of the primal error and of lambda d,
+//   w_p (4096 / n) sum_blocks (Rx^2 + Rd^2)
+// (white-noise errors weigh as in the pixel terms, smooth ones 64 times more).
+OPYX_D float warm_div(int H, int W, const float* out, const float* tgt, int64_t i, int x, int y) {
+  float d = 0.f;
+  if (y < H - 1) d += out[3 * i + 1] - tgt[3 * i + 1];
+  if (y > 0) d -= out[3 * (i - W) + 1] - tgt[3 * (i - W) + 1];
+  if (x < W - 1) d += out[3 * i + 2] - tgt[3 * i + 2];
+  if (x > 0) d -= out[3 * (i - 1) + 2] - tgt[3 * (i - 1) + 2];
+  return d;
+}
+
+__global__ void k_warm_pool(int B, int H, int W, const float* __restrict__ out,
+                            const float* __restrict__ tgt, const float* __restrict__ lam,
+                            float* __restrict__ pooled) {
+  const int hb = H / 8, wb = W / 8;
+  const int64_t total = (int64_t)B * hb * wb;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int bx = (int)(k % wb), by = (int)((k / wb) % hb);
+    const int64_t n = k / ((int64_t)hb * wb);
+    const float l = lam[n];
+    float rx = 0.f, rd = 0.f;
+    for (int yy = 8 * by; yy < 8 * by + 8; ++yy)
+      for (int xx = 8 * bx; xx < 8 * bx + 8; ++xx) {
+        const int64_t i = (n * H + yy) * W + xx;
+        rx += out[3 * i] - tgt[3 * i];
+        rd += l * warm_div(H, W, out, tgt, i, xx, yy);
+      }
+    pooled[2 * k] = rx * (1.f / 64.f);
+    pooled[2 * k + 1] = rd * (1.f / 64.f);
+  }
+}
+
+// Pass 1: c = 2 w_div lambda^2 d / n (+ the pooled term's share) into `scr`,
+// loss partials per block.
+__global__ void k_warm_loss1(int B, int H, int W, const float* __restrict__ out,
+                             const float* __restrict__ tgt, const float* __restrict__ lam, float w_x,
+                             float w_div, float w_u, float w_p, double inv_n,
+                             const float* __restrict__ pooled, float* __restrict__ scr,
+                             double* __restrict__ part) {
+  const int64_t total = (int64_t)B * H * W;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % W), y = (int)((i / W) % H);
+    const float l = lam[i / ((int64_t)H * W)];
+    const float r0 = out[3 * i] - tgt[3 * i];
+    const float e0 = out[3 * i + 1] - tgt[3 * i + 1], e1 = out[3 * i + 2] - tgt[3 * i + 2];
+    const float d = warm_div(H, W, out, tgt, i, x, y);
+    const float ld = l * d;
+    acc += (double)(w_x * r0 * r0 + w_div * ld * ld + w_u * (e0 * e0 + e1 * e1));
+    float c = (float)(2.0 * inv_n) * w_div * l * ld;
+    if (w_p != 0.f) {
+      const int64_t k = ((i / ((int64_t)H * W)) * (H / 8) + y / 8) * (W / 8) + x / 8;
+      const float rd = pooled[2 * k + 1];
+      c += (float)(128.0 * inv_n) * w_p * l * rd;
+      if ((x & 7) == 0 && (y & 7) == 0) {
+        const float rx = pooled[2 * k];
+        acc += (double)(4096.f * w_p * (rx * rx + rd * rd));
+      }
+    }
+    scr[i] = c;
+  }
+  acc = warp_reduce(RED_SUM, acc);
+  __shared__ double wr[32];
+  if ((threadIdx.x & 31) == 0) wr[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) s += wr[w2];
+    part[blockIdx.x] = s * inv_n;
+  }
+}
+
+// Pass 2: grad o0 = 2 w_x r0 / n; grad e_t = 2 w_u e_t / n + (div^T c)_t,
+// where div^T c = c[i] - c[i + s_t] if i + s_t is inside the image, else 0
+// (minus the forward gradient of c): the adjoint of the sum above.
+__global__ void k_warm_loss2(int B, int H, int W, const float* __restrict__ out,
+                             const float* __restrict__ tgt, float w_x, float w_u, float w_p,
+                             double inv_n, const float* __restrict__ pooled,
+                             const float* __restrict__ scr, float* __restrict__ grad) {
+  const int64_t total = (int64_t)B * H * W;
+  const float s2 = (float)(2.0 * inv_n);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % W), y = (int)((i / W) % H);
+    const float c = scr[i];
+    // d_j depends on e0[i] with +1 (j = i, y < H-1) and -1 (j = i + W, y+1 > 0)
+    float g0 = 0.f, g1 = 0.f;
+    if (y < H - 1) g0 = c - scr[i + W];
+    if (x < W - 1) g1 = c - scr[i + 1];
+    float gx = s2 * w_x * (out[3 * i] - tgt[3 * i]);
+    if (w_p != 0.f) {
+      const int64_t k = ((i / ((int64_t)H * W)) * (H / 8) + y / 8) * (W / 8) + x / 8;
+      gx += (float)(128.0 * inv_n) * w_p * pooled[2 * k];
+    }
+    grad[3 * i] = gx;
+    grad[3 * i + 1] = s2 * w_u * (out[3 * i + 1] - tgt[3 * i + 1]) + g0;
+    grad[3 * i + 2] = s2 * w_u * (out[3 * i + 2] - tgt[3 * i + 2]) + g1;
+  }
+}
+
+// Proposal: x0 = f + o0, y0 = lambda * (o1, o2) / max(1, |(o1, o2)|).
+__global__ void k_warm_unpack(int64_t npix, int64_t hw, const float* __restrict__ f,
+                              const float* __restrict__ lam, const float* __restrict__ out,
+                              float* __restrict__ x0, float* __restrict__ y0) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float l = lam[i / hw];
+    x0[i] = f[i] + out[3 * i];
+    const float u0 = out[3 * i + 1], u1 = out[3 * i + 2];
+    const float n = sqrtf(u0 * u0 + u1 * u1);
+    const float s = l / (n > 1.f ? n : 1.f);
+    y0[2 * i] = s * u0;
+    y0[2 * i + 1] = s * u1;
+  }
+}
+
 // Adam (Kingma & Ba 2015) on FP32 master weights; optionally refreshes the
 // bf16 copy used by the forward convolutions and the tap-flipped,
 // in/out-transposed bf16 copy used by the input-gradient convolutions.
@@ -954,6 +1082,37 @@ int opyx_mse(int64_t n, int K, const float* pred, const float* tgt, const float*
              double* partials, int nparts, void* stream) {
   if (n < 1 || K < 1 || !pred || !tgt || !wk || !grad || !partials || nparts < 1) return OPYX_ERR_ARG;
   k_mse<<<nparts, 256, 0, (cudaStream_t)stream>>>(n, K, pred, tgt, wk, 1.0 / (double)n, grad, partials);
+  return check_launch();
+}
+
+int opyx_warm_loss(int B, int H, int W, const float* out, const float* tgt, const float* lam,
+                   double w_x, double w_div, double w_u, double w_pool, float* grad, float* scratch,
+                   double* partials, int nparts, void* stream) {
+  if (B < 1 || H < 2 || W < 2 || !out || !tgt || !lam || !grad || !scratch || !partials || nparts < 1)
+    return OPYX_ERR_ARG;
+  if (w_pool != 0.0 && (H % 8 || W % 8)) return OPYX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const double inv_n = 1.0 / ((double)B * H * W);
+  const int64_t total = (int64_t)B * H * W;
+  float* pooled = scratch + total;
+  if (w_pool != 0.0) {
+    const int64_t nb = total / 64;
+    k_warm_pool<<<grid_for(nb, 256), 256, 0, s>>>(B, H, W, out, tgt, lam, pooled);
+    OPYX_CHECK_LAUNCH();
+  }
+  k_warm_loss1<<<nparts, 256, 0, s>>>(B, H, W, out, tgt, lam, (float)w_x, (float)w_div, (float)w_u,
+                                      (float)w_pool, inv_n, pooled, scratch, partials);
+  OPYX_CHECK_LAUNCH();
+  k_warm_loss2<<<grid_for(total, 256), 256, 0, s>>>(B, H, W, out, tgt, (float)w_x, (float)w_u,
+                                                    (float)w_pool, inv_n, pooled, scratch, grad);
+  return check_launch();
+}
+
+int opyx_warm_unpack(int B, int64_t hw, const float* f, const float* lam, const float* out, float* x0,
+                     float* y0, void* stream) {
+  if (B < 1 || hw < 1 || !f || !lam || !out || !x0 || !y0) return OPYX_ERR_ARG;
+  const int64_t n = (int64_t)B * hw;
+  k_warm_unpack<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, hw, f, lam, out, x0, y0);
   return check_launch();
 }
 

@@ -149,13 +149,24 @@ class BatchROF(object):
         return best[1]
 
     # ---------------------------------------------------------------- solve
-    def solve(self, maxiter=5000):
+    def solve(self, maxiter=5000, init=None):
         """Iterate until every image passed its stop test or `maxiter`
         iterations; returns per image a dict with the reference's info keys
-        and `iter`.  States: `self.state(i)` (x as an (H, W, C) array)."""
+        and `iter`.  States: `self.state(i)` (x as an (H, W, C) array),
+        `self.dual(i)` (y as (H, W, 2, C)).  `init`: optional starting
+        points, a sequence of (x, y) per image (device tensors or arrays of
+        N*C and N*2*C values; the reference's `continue_at`,
+        opymize/solvers/pdhg.py:254-255); zero otherwise."""
         if self.rows_per_item is None:
             self.autotune()
         self._reset()
+        if init is not None:
+            t = torch()
+            for arr, (x0, y0) in zip(self.arrays, init):
+                for key, v in (("x", x0), ("y", y0)):
+                    src = v if hasattr(v, "data_ptr") else t.from_numpy(
+                        np.ascontiguousarray(v, dtype=np.float32))
+                    arr[key].t.copy_(src.reshape(-1))
         names = _lib.ROF_INFO_FIELDS
         i_done, i_fault = names.index("done"), names.index("fault")
         active = np.ones(self.n, np.uint8)
@@ -193,6 +204,10 @@ class BatchROF(object):
     def state(self, i):
         H, W, C = self.dims[i]
         return self.arrays[i]["x"].get().reshape(H, W, C)
+
+    def dual(self, i):
+        H, W, C = self.dims[i]
+        return self.arrays[i]["y"].get().reshape(H, W, 2, C)
 
     def pixels(self):
         return sum(H * W for H, W, _ in self.dims)
