@@ -272,6 +272,96 @@ def sublabel_case(a, iters=200):
             "note": "wall time of solve() incl. setup of steps and one final gap"}
 
 
+def batch_case(a):
+    """The batched configuration: 512 independent 2-D instances, sides
+    log-uniform in [64, 1024], aspect U[0.5, 2], lambda U[0.02, 0.3], noise
+    sigma U[0.05, 0.2], FP32; every instance retires at its own relgap 1e-4;
+    rows per work item chosen by the autotuner (BatchROF)."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.solvers import BatchROF
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    t = torch()
+    rng = np.random.default_rng(a.seed)
+    imgs, lbds = [], []
+    for k in range(512):
+        side = np.exp(rng.uniform(np.log(64), np.log(1024)))
+        asp = rng.uniform(0.5, 2.0)
+        H = max(8, int(round(side)))
+        W = max(4, int(round(side * asp / 4)) * 4)
+        imgs.append(piecewise_constant((H, W), 1, sigma=rng.uniform(0.05, 0.2), seed=1000 + k))
+        lbds.append(rng.uniform(0.02, 0.3))
+    b = BatchROF(imgs, lbds, tol=1e-4, granularity=10)
+    b.autotune()
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    info = b.solve(maxiter=20000)
+    t.cuda.synchronize()
+    el = time.perf_counter() - t0
+    its = np.array([d["iter"] for d in info])
+    npx = np.array([im.shape[0] * im.shape[1] for im in imgs])
+    byts = float((28.0 * npx * its).sum())     # single sweep: 4 N (3C + 2K) bytes, C = 1, K = 2
+    peak = measured_peaks().get("hbm_gbs")
+    gbs = byts / el / 1e9
+    return {"workload": "512 ROF instances, sides log-uniform [64, 1024], aspect U[0.5, 2], "
+                        "lambda U[0.02, 0.3], sigma U[0.05, 0.2], fp32, retire at relgap 1e-4",
+            "solves_per_s": round(len(imgs) / el, 2), "wall_s": round(el, 3),
+            "converged": int(sum(d["converged"] for d in info)), "maxiter": 20000,
+            "iters_median": float(np.median(its)), "iters_max": int(its.max()),
+            "pixels": int(npx.sum()), "sum_bytes_per_wall_GBps": round(gbs, 1),
+            "frac_of_measured_hbm": round(gbs / peak, 3) if peak else None,
+            "rows_per_item": b.rows_per_item, "launches": b.launches,
+            "data": "synthetic piecewise-constant images, resident in HBM"}
+
+
+def warm_start_case(a, n_eval=32):
+    """The learned warm start on 512^2: the committed U-Net's proposals vs
+    the zero start on held-out seeds, same solver (BatchROF) and stop test;
+    plus the tcgen05 convolutions' throughput (forward of a 32-image batch,
+    and the largest layer alone) against the measured bf16 peak."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.warmstart import UNet, evaluate, instances
+    t = torch()
+    path = os.path.join(ROOT, "opymize_gb300", "warmstart", "unet512.npz")
+    net = UNet.load(path)
+    seeds = range(3 * 10 ** 6, 3 * 10 ** 6 + n_eval)
+    res = {"workload": "ROF 512^2, lambda U[0.02, 0.3], sigma U[0.05, 0.2]: U-Net proposal "
+                       "(0.64M params, bf16 tensor cores) + fused PDHG vs zero start",
+           "held_out": n_eval}
+    for tol in (1e-4, 1e-3):
+        ev = evaluate(net, seeds, S=512, tol=tol)
+        res["relgap_%g" % tol] = {
+            "iters_cold_mean": float(np.mean(ev["iters_cold"])),
+            "iters_warm_mean": float(np.mean(ev["iters_warm"])),
+            "solve_cold_ms": round(1e3 * ev["solve_cold_s"], 2),
+            "solve_warm_ms": round(1e3 * ev["solve_warm_s"], 2),
+            "net_ms": round(1e3 * ev["net_s"], 2),
+            "time_ratio_cold_over_warm": round(ev["speedup"], 3),
+            "converged": [ev["converged_cold"], ev["converged_warm"]]}
+    B, S = 32, 512
+    f, lam = instances(range(B), S)
+    fd, ld = t.from_numpy(f).cuda(), t.from_numpy(lam).cuda()
+    for _ in range(3):
+        net.forward(fd, ld)
+    e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        net.forward(fd, ld)
+    e1.record()
+    t.cuda.synchronize()
+    fwd_s = e0.elapsed_time(e1) / 1e3 / 5
+    peak = measured_peaks().get("bf16_tflops")
+    layer_s, layer_fl = net.time_conv("d0", B, S)
+    res["network"] = {"batch": B, "forward_ms": round(1e3 * fwd_s, 3),
+                      "forward_conv_TFLOPs": round(net.conv_flops(B, S) / fwd_s / 1e12, 1),
+                      "largest_layer": "d0 (64 -> 32 channels at 512^2)",
+                      "layer_us": round(1e6 * layer_s, 1),
+                      "layer_TFLOPs": round(layer_fl / layer_s / 1e12, 1),
+                      "layer_frac_of_measured_bf16": round(layer_fl / layer_s / 1e12 / peak, 3)
+                      if peak else None}
+    net.check_fault()
+    return res
+
+
 def e2e_solve(a, f):
     """The public-API call a user makes, host data in and out."""
     from opymize_gb300.functionals import SSD, HuberL1Norms
@@ -436,7 +526,9 @@ def run_gpu_arm(a, world, rank, local):
             # the other configurations of the path, outside the headline metric
             del rs
             out["other_workloads"] = {"volume_256x256x256": volume_case(a),
-                                      "sublabel_512x512_L16": sublabel_case(a)}
+                                      "sublabel_512x512_L16": sublabel_case(a),
+                                      "batched_512_instances": batch_case(a),
+                                      "warm_start_512x512": warm_start_case(a)}
         if world == 1 and not a.no_cpu:
             cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs_iters)
             out["cpu_baseline"] = {

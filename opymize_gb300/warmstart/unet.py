@@ -326,6 +326,37 @@ class UNet(object):
                   stream_ptr())
         return x0, y0
 
+    # ------------------------------------------------------------ measurement
+    def conv_flops(self, B, S, backward=False):
+        """Tensor-core FLOPs of the 3x3 convolutions as executed (e0a with
+        its 32 padded input channels): forward, or forward + input gradient
+        (every layer but e0a) + weight gradient."""
+        fwd = sum(2.0 * B * (S >> l[9]) ** 2 * l[4] * l[5] * 9 for l in LAYERS)
+        if not backward:
+            return fwd
+        dgrad = sum(2.0 * B * (S >> l[9]) ** 2 * l[4] * l[5] * 9 for l in LAYERS if l[0] != "e0a")
+        return 2 * fwd + dgrad
+
+    def time_conv(self, name, B, S, reps=20):
+        """Mean time (s) of one forward launch of layer `name` on the
+        current buffers, CUDA events on the current stream."""
+        t = torch()
+        b = self.buffers(B, S)
+        _, src, _, _, cin, cout, dst, _, _, lev = LAYER[name]
+        d = self._desc(name, B, S, b[src], b[dst], b["z." + name], bias=self.params[name + ".b"],
+                       w=self.wb[name])
+        s = stream_ptr()
+        for _ in range(3):
+            _lib.call("opyx_conv3x3", C.byref(d), s)
+        e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            _lib.call("opyx_conv3x3", C.byref(d), s)
+        e1.record()
+        t.cuda.synchronize()
+        flops = 2.0 * B * (S >> lev) ** 2 * cin * cout * 9
+        return e0.elapsed_time(e1) / 1e3 / reps, flops
+
     # -------------------------------------------------------------- storage
     def state_dict(self):
         return {k: v.detach().cpu().numpy() for k, v in self.params.items()}
