@@ -211,3 +211,39 @@ class BatchROF(object):
 
     def pixels(self):
         return sum(H * W for H, W, _ in self.dims)
+
+
+def _main(argv=None):
+    """A seeded mixed-size batch (sides log-uniform in [64, 1024], aspect
+    U[0.5, 2], lambda U[0.02, 0.3], sigma U[0.05, 0.2]) solved for a few
+    iterations -- a small case for profilers:
+
+        python -m opymize_gb300.solvers.batch --n 96 --maxiter 10
+    """
+    import argparse
+    import json
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=96)
+    ap.add_argument("--maxiter", type=int, default=10)
+    ap.add_argument("--rows", type=int, default=8)
+    ap.add_argument("--tol", type=float, default=1e-4)
+    a = ap.parse_args(argv)
+    rng = np.random.default_rng(0)
+    imgs, lbds = [], []
+    for k in range(a.n):
+        side = np.exp(rng.uniform(np.log(64), np.log(1024)))
+        asp = rng.uniform(0.5, 2.0)
+        H = max(8, int(round(side)))
+        W = max(4, int(round(side * asp / 4)) * 4)
+        imgs.append(piecewise_constant((H, W), 1, sigma=rng.uniform(0.05, 0.2), seed=1000 + k))
+        lbds.append(rng.uniform(0.02, 0.3))
+    b = BatchROF(imgs, lbds, tol=a.tol, granularity=10, rows_per_item=a.rows)
+    info = b.solve(maxiter=a.maxiter)
+    torch().cuda.synchronize()
+    print(json.dumps({"instances": a.n, "pixels": b.pixels(), "launches": b.launches,
+                      "iters": max(d["iter"] for d in info)}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -30,11 +30,29 @@ def main(argv=None):
     ap.add_argument("--eval-tols", default="1e-4", help="comma-separated relative gaps")
     ap.add_argument("--init", default=None, help="start from these weights")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only run this many training steps on --batch seeded images (for profilers)")
     a = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)
     t0 = time.perf_counter()
     net = UNet.load(a.init) if a.init else UNet(seed=0)
     res = dict(size=a.size, params=net.nparams())
+    if a.profile_steps > 0:
+        import torch
+        from opymize_gb300.warmstart import instances
+        f, lam = instances(range(a.batch), a.size)
+        fd, ld = torch.from_numpy(f).cuda(), torch.from_numpy(lam).cuda()
+        tgt = torch.zeros(a.batch, a.size, a.size, 3, device="cuda")
+        for _ in range(a.profile_steps):
+            net.forward(fd, ld)
+            net.loss_warm(tgt)
+            net.backward()
+            net.adam_step(lr=a.lr)
+        torch.cuda.synchronize()
+        net.check_fault()
+        res["profile_steps"] = a.profile_steps
+        print(json.dumps(res))
+        return
     if a.train > 0:
         data = make_dataset(range(a.train), S=a.size, tol=a.data_tol, maxiter=a.data_maxiter)
         its = np.array([d["iter"] for d in data["infos"]])
