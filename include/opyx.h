@@ -393,6 +393,10 @@ size_t opyx_rof_info_offset(void);
  * xgrad = A^T y of the initial y.  x, y hold the starting point. */
 int opyx_rof_init(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);
 /* Run `iters` PDHG iterations (pdhg.py:124-187). */
+/* 1 if opyx_rof_iterate runs single sweeps for this problem and buffers
+ * (FP32, constant or preconditioned steps, y2 given; 2-D, or 3-D with one
+ * channel, rows of 128, 256 or 512 pixels and no mask), else 0. */
+int opyx_rof_uses_sweep(const opyx_rof_problem* p, const opyx_rof_buffers* b);
 int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
                      void* stream);
 /* One pass of an iteration (0 = primal pass A, 1 = dual pass B, 2 = the

@@ -8,6 +8,7 @@
 #include "rof_vec.cuh"
 #include "rof_pipe.cuh"
 #include "rof_sweep.cuh"
+#include "rof_sweep3.cuh"
 
 namespace opyx {
 namespace rof {
@@ -272,12 +273,17 @@ struct PipeLaunch<float, D, C> {
   }
 };
 
-// Single-sweep iterations (rof_sweep.cuh): 2-D FP32 problems with constant
-// or preconditioned steps whose caller gave the second dual buffer y2.
+// Single-sweep iterations (rof_sweep.cuh, rof_sweep3.cuh): FP32 problems
+// with constant or preconditioned steps whose caller gave the second dual
+// buffer y2; 2-D any channel count, 3-D one channel, rows of 128, 256 or
+// 512 pixels, no mask.
 template <typename T, int D>
 static bool sweep_ok(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
-  return D == 2 && p->steps != OPYX_STEPS_ADAPTIVE && b->y2 && !(((uintptr_t)b->y2) & 15) &&
-         pipe_ok<T>(p, b);
+  if (p->steps == OPYX_STEPS_ADAPTIVE || !b->y2 || (((uintptr_t)b->y2) & 15) || !pipe_ok<T>(p, b))
+    return false;
+  if (D == 2) return true;
+  const int64_t nl = p->dims[2];
+  return D == 3 && p->nchannels == 1 && !b->mask && (nl == 128 || nl == 256 || nl == 512);
 }
 
 template <typename T, int D, int C>
@@ -307,6 +313,47 @@ struct SweepLaunch<float, 2, C> {
     if (g.nl <= 128) go<128>(g, a, s);
     else if (g.nl <= 256) go<256>(g, a, s);
     else go<kPipeTW>(g, a, s);
+  }
+};
+
+// 3-D sweep: TY = 4 rows per plane tile; the planes are cut into ranges so
+// that the work items fill whole waves of resident CTAs, traded against the
+// halo plane each range recomputes.
+constexpr int kSweep3TY = 4;
+
+template <int C>
+struct SweepLaunch<float, 3, C> {
+  template <int TW>
+  static void go(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+    constexpr int TY = kSweep3TY, P = 4;
+    constexpr int threads = (TY + 1) * (TW / P);
+    constexpr int smem = Sweep3Smem<TW, TY>::bytes;
+    static int per_sm = -1;
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep3<TW, TY, P>, smem, threads);
+    const int64_t R = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
+    const int64_t Z = g.n[0];
+    const int nyt = (int)((g.n[1] + TY - 1) / TY);
+    int best_nc = 1;
+    double best = 1e30;
+    for (int64_t nc = 1; nc <= Z; ++nc) {
+      const int64_t zc = (Z + nc - 1) / nc;
+      if (nc > 1 && zc < 4) break;
+      const double items = (double)nyt * (double)((Z + zc - 1) / zc);
+      const double waves = items / (double)R;
+      const double fill = waves >= 1.0 ? ceil(waves) / waves : 1.0 / waves;
+      const double cost = fill * (1.0 + 1.0 / (double)zc);
+      if (cost < best) { best = cost; best_nc = (int)nc; }
+    }
+    const int ZC = (int)((Z + best_nc - 1) / best_nc);
+    const int64_t items = (int64_t)nyt * ((Z + ZC - 1) / ZC);
+    const int64_t grid = items < R ? items : R;
+    k_sweep3<TW, TY, P><<<(unsigned)grid, threads, smem, s>>>(g, a, ZC, nyt);
+  }
+  static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+    if (C != 1) return;
+    if (g.nl == 128) go<128>(g, a, s);
+    else if (g.nl == 256) go<256>(g, a, s);
+    else go<512>(g, a, s);
   }
 };
 
@@ -467,6 +514,14 @@ int opyx_rof_init(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* st
   st = check_launch();
   if (st) return st;
   return dispatch(p, [&](auto r) { return decltype(r)::init(p, b, s); });
+}
+
+int opyx_rof_uses_sweep(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
+  if (!p || !b || validate(p, b)) return 0;
+  if (p->dtype != OPYX_F32) return 0;
+  if (p->ndim == 2) return sweep_ok<float, 2>(p, b) ? 1 : 0;
+  if (p->ndim == 3) return sweep_ok<float, 3>(p, b) ? 1 : 0;
+  return 0;
 }
 
 int opyx_rof_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,

@@ -188,10 +188,11 @@ class PDHG(object):
         gp = DeviceArray.empty((N * C,), dtype) if adaptive else None
         wsb = lib.opyx_rof_workspace_size()
         ws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
-        # second dual buffer: 2-D FP32 iterations then run as one sweep over
-        # HBM each (the library falls back to two passes where it cannot)
+        # second dual buffer: FP32 iterations then run as one sweep over HBM
+        # each (2-D; 3-D with one channel) -- the library falls back to two
+        # passes where it cannot
         y2 = DeviceArray.empty((y.size,), dtype) \
-            if dtype == np.float32 and D == 2 and not adaptive else None
+            if dtype == np.float32 and (D == 2 or (D == 3 and C == 1)) and not adaptive else None
         p = self._rof_problem(dtype, steps)
         b = _lib.opyx_rof_buffers()
         b.x, b.xbar, b.y, b.f = x.ptr, xbar.ptr, y.ptr, fdev.ptr
@@ -402,6 +403,7 @@ class _FusedLoop(object):
         self.graphs = {}
         self.host = None
         self.launches = 0      # kernel launches queued so far
+        self.sweeps = bool(_lib.load().opyx_rof_uses_sweep(p, b))
 
     def chunk(self, n, check):
         if check and self.use_graph:
@@ -414,8 +416,7 @@ class _FusedLoop(object):
             if check:
                 _lib.call("opyx_rof_gap", self.p, self.b, stream_ptr())
         p = self.p
-        if self.b.y2 and p.ndim == 2 and p.dtype == _lib.OPYX_F32 and \
-                p.steps != _lib.STEPS["adaptive"] and not (p.flags & 3):
+        if self.sweeps:
             kernels = (n // 2) * 2 + (n % 2) * 2       # sweeps; an odd count ends two-pass
         else:
             kernels = n * (3 if p.steps == _lib.STEPS["adaptive"] else 2)

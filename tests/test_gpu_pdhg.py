@@ -313,3 +313,84 @@ def test_single_sweep_matches_two_passes_bitwise(dims, C, huber, steps, masked, 
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
     assert np.abs(out[1][1]).max() > 0
+
+
+@pytest.mark.parametrize("dims,huber,steps", [((7, 30, 128), 0.0, "precond"),
+                                              ((5, 8, 256), 0.01, "precond"),
+                                              ((33, 19, 512), 0.0, "const"),
+                                              ((64, 64, 256), 0.02, "precond"),
+                                              ((1, 9, 128), 0.0, "precond")])
+@pytest.mark.parametrize("iters", [1, 6, 7])
+def test_single_sweep_3d_matches_two_passes(dims, huber, steps, iters):
+    """3-D one-channel iterations as one sweep (plane tiles streamed along z,
+    xbar of two planes on chip) against the two-pass kernels, for ragged
+    row tiles, several plane ranges (halo planes), a single plane, constant
+    and preconditioned steps, Huber, odd and even counts.  The per-voxel
+    formulas are those of the two passes, but the compiler fuses some
+    multiply-adds differently in the two kernels, so values differ in the
+    last bit (measured <= 3e-8 absolute): the bar is 1e-6 relative."""
+    from opymize_gb300 import _lib
+    from opymize_gb300.gpuarray import DeviceArray, stream_ptr
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG
+    f = piecewise_constant(dims, 1, sigma=0.1, seed=5)
+    N, D = int(np.prod(dims)), 3
+    Fg = HuberL1Norms(N, (1, D), 0.08, huber) if huber > 0 else L1Norms(N, (1, D), 0.08)
+    s = PDHG(SSD(f.reshape(N, 1)), Fg, GradientOp(dims, 1, scheme="forward"))
+    s.constvars.update(theta=1.0, tau=0.2, sigma=0.3)
+    out = []
+    for sweep in (False, True):
+        p = s._rof_problem(np.float32, steps)
+        x = DeviceArray.zeros((N,), np.float32)
+        y = DeviceArray.zeros((N * D,), np.float32)
+        xbar = DeviceArray.zeros((N,), np.float32)
+        y2 = DeviceArray.zeros((N * D,), np.float32)
+        ws = DeviceArray.zeros(((_lib.load().opyx_rof_workspace_size() + 7) // 8,), np.float64)
+        fd = s.g.f_dev(np.float32)
+        b = _lib.opyx_rof_buffers()
+        b.x, b.xbar, b.y, b.f, b.ws = x.ptr, xbar.ptr, y.ptr, fd.ptr, ws.ptr
+        b.y2 = y2.ptr if sweep else None
+        assert _lib.load().opyx_rof_uses_sweep(p, b) == int(sweep)
+        _lib.call("opyx_rof_init", p, b, stream_ptr())
+        b2 = _lib.opyx_rof_buffers.from_buffer_copy(b)
+        b2.y2 = None
+        _lib.call("opyx_rof_iterate", p, b2, 3, stream_ptr())
+        _lib.call("opyx_rof_iterate", p, b, iters, stream_ptr())
+        out.append((x.get().copy(), y.get().copy(), ws.get().copy()))
+    assert rel(out[1][0], out[0][0]) <= 1e-6
+    assert rel(out[1][1], out[0][1]) <= 1e-6
+    assert np.abs(out[1][1]).max() > 0
+    off = _lib.load().opyx_rof_info_offset() // 8
+    assert out[1][2][off + _lib.ROF_INFO_FIELDS.index("fault")] == 0
+
+
+def test_single_sweep_3d_matches_oracle():
+    """The public solver on a volume that takes the 3-D sweep (rows of 128
+    voxels, one channel, preconditioned steps, FP32) against the FP64 oracle
+    after 60 iterations: relative L2 <= 1e-5 for x and y, and the gap."""
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.solvers import PDHG
+    from opymize_gb300.functionals import SSD, L1Norms
+    from opymize_gb300.linear import GradientOp
+    dims = (6, 10, 128)
+    f = piecewise_constant(dims, 1, sigma=0.1, seed=23)
+    N = int(np.prod(dims))
+    s = PDHG(SSD(f.reshape(N, 1)), L1Norms(N, (1, 3), 0.08), GradientOp(dims, 1, scheme="forward"))
+    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=60,
+            granularity=10)
+    assert s.path == "fused" and s._fused["y2"] is not None
+    assert _lib_uses_sweep(s)
+    so = oracle.PDHG(oracle.SSD(f.reshape(N, 1)), oracle.L1Norms(N, (1, 3), 0.08),
+                     oracle.Gradient(dims, 1, "forward"))
+    so.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=60, granularity=10)
+    assert rel(s.state[0].ravel(), so.state[0].ravel()) <= 1e-5
+    assert rel(s.state[1].ravel(), so.state[1].ravel()) <= 1e-5
+    assert abs(s.info["relgap"] - so.info["relgap"]) <= 2e-6 + 1e-4 * abs(so.info["relgap"])
+
+
+def _lib_uses_sweep(s):
+    from opymize_gb300 import _lib
+    fz = s._fused
+    return bool(_lib.load().opyx_rof_uses_sweep(fz["problem"], fz["buffers"]))
