@@ -316,10 +316,12 @@ struct SweepLaunch<float, 2, C> {
   }
 };
 
-// 3-D sweep: TY = 4 rows per plane tile; the planes are cut into ranges so
-// that the work items fill whole waves of resident CTAs, traded against the
-// halo plane each range recomputes.
-constexpr int kSweep3TY = 4;
+// 3-D sweep: TY = 3 rows per plane tile (measured on 256^3: TY = 1, 2, 3,
+// 4, 8 gave 151, 121, 109, 127, 148 us -- three rows keep three CTAs per SM
+// at 70 KB of shared memory); the planes are cut into ranges so that the
+// work items fill whole waves of resident CTAs, traded against the halo
+// plane each range recomputes.
+constexpr int kSweep3TY = 3;
 
 template <int C>
 struct SweepLaunch<float, 3, C> {
