@@ -1,0 +1,43 @@
+"""A fused ROF solve of a seeded synthetic image or volume for a fixed
+number of iterations -- a small, repeatable case for profilers:
+
+    python -m opymize_gb300.solvers --dims 256 256 256 --iters 20
+    python -m opymize_gb300.solvers --dims 2048 2048 --channels 3 --huber 0.01 --lbd 0.05
+"""
+
+import argparse
+import json
+
+import numpy as np
+
+from opymize_gb300.functionals import SSD, L1Norms, HuberL1Norms
+from opymize_gb300.gpuarray import torch
+from opymize_gb300.linear import GradientOp
+from opymize_gb300.solvers import PDHG
+from opymize_gb300.tools.synthetic import piecewise_constant
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dims", type=int, nargs="+", default=[256, 256, 256])
+    ap.add_argument("--channels", type=int, default=1)
+    ap.add_argument("--lbd", type=float, default=0.08)
+    ap.add_argument("--huber", type=float, default=0.0)
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--steps", default="precond")
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    dims, C = tuple(a.dims), a.channels
+    N, D = int(np.prod(dims)), len(dims)
+    f = piecewise_constant(dims, C, sigma=0.1, seed=a.seed)
+    F = HuberL1Norms(N, (C, D), a.lbd, a.huber) if a.huber > 0 else L1Norms(N, (C, D), a.lbd)
+    s = PDHG(SSD(f.reshape(N, C)), F, GradientOp(dims, C, scheme="forward"))
+    s.solve(steps=a.steps, precision="float", term_pd_gap=1e-300, term_maxiter=a.iters,
+            granularity=a.iters)
+    torch().cuda.synchronize()
+    print(json.dumps({"dims": list(dims), "channels": C, "path": s.path, "iters": s.info["iter"],
+                      "relgap": s.info["relgap"]}))
+
+
+if __name__ == "__main__":
+    main()
