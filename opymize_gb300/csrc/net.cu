@@ -17,8 +17,9 @@
 // Weight gradient as an implicit GEMM with the pixel axis as K:
 // dW[tap][co][ci] = sum_p x[p + off(tap), ci] * dy[p, co].  Both operands
 // are read in their natural NHWC layout, which for this product is
-// MN-major (channels contiguous, pixels along K); a CTA covers one tap, 128
-// input channels and a contiguous range of pixel tiles and writes an FP32
+// MN-major (channels contiguous, pixels along K); a CTA covers 128
+// accumulator rows (one tap and 128 input channels, or several taps of a
+// narrower input) and a contiguous range of pixel tiles and writes an FP32
 // partial that a second kernel sums over the ranges in a fixed order.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -216,45 +217,69 @@ k_conv3x3(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
 }
 
 // ------------------------------------------------------------ weight grad
-constexpr int kWgStages = 3;
-
+// The 128 rows of a CTA's accumulator are four 32-channel blocks of the
+// input; with fewer than 128 input channels each block takes another tap
+// (taps_per_group = 128 / cin: 4 taps at 32 channels, 2 at 64), so no MMA
+// row is wasted on channels that do not exist.  Stages by accumulator width:
+// as many as fit in 200 KB of shared memory (5, 4, 3 for N = 32, 64, 128).
 template <int N>
 struct WgSmem {
   static constexpr int BLK = kTileM * kChunk * 2;      // 128 pixels x 32 channels: 8 KB
-  static constexpr int A = 4 * BLK;                    // 128 input channels
+  static constexpr int A = 4 * BLK;                    // 4 blocks of 32 input channels
   static constexpr int Bb = (N / kChunk) * BLK;        // N output channels
   static constexpr int STAGE = A + Bb;
-  static constexpr int bytes = kWgStages * STAGE + 1024;
+  static constexpr int stages = N == 32 ? 5 : N == 64 ? 4 : 3;
+  static constexpr int bytes = stages * STAGE + 1024;
   static constexpr int cols = N <= 32 ? 32 : N <= 64 ? 64 : 128;
 };
 
 struct WgArgs {
   int32_t B, H, W, Wt, Ht;
   int32_t cin, in_off, cout;
+  int32_t tpg, ngroups;           // taps per group, tap groups
   int32_t tiles, tiles_per_cta;   // pixel tiles in total / per CTA
-  float* ws;                      // [split][9][ci_tiles * 128][cout]
+  float* ws;                      // [split][9][cin][cout]
   unsigned* fault;
 };
+
+// Tap and first input channel of accumulator block b (0..3) for tap group
+// `grp` and channel tile mt; false if the block holds nothing.
+OPYX_D bool wg_block(const WgArgs& p, int grp, int mt, int b, int* tap, int* c0) {
+  if (p.tpg > 1) {
+    const int per = p.cin / kChunk;            // blocks per tap
+    *tap = grp * p.tpg + b / per;
+    *c0 = (b % per) * kChunk;
+    return *tap < 9;
+  }
+  *tap = grp;
+  *c0 = (mt * 4 + b) * kChunk;
+  return *c0 < p.cin;
+}
 
 template <int N>
 __global__ void __launch_bounds__(kConvThreads, 1)
 k_conv3x3_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dmap,
                 const WgArgs p) {
   using S = WgSmem<N>;
+  constexpr int NS = S::stages;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full[kWgStages], empty[kWgStages], accf;
+  __shared__ __align__(8) uint64_t full[NS], empty[NS], accf;
   __shared__ uint32_t tmem_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tap = blockIdx.x % 9, split = blockIdx.x / 9, mt = blockIdx.y;
+  const int grp = blockIdx.x % p.ngroups, split = blockIdx.x / p.ngroups, mt = blockIdx.y;
   const int t0 = split * p.tiles_per_cta;
   const int t1 = t0 + p.tiles_per_cta < p.tiles ? t0 + p.tiles_per_cta : p.tiles;
-  const int ci_blocks = (p.cin - mt * kTileM) / kChunk < 4 ? (p.cin - mt * kTileM) / kChunk : 4;
-  const unsigned stage_bytes = (unsigned)((ci_blocks + N / kChunk) * S::BLK);
+  int nblk = 0;
+  for (int b = 0; b < 4; ++b) {
+    int tp, c0;
+    nblk += wg_block(p, grp, mt, b, &tp, &c0) ? 1 : 0;
+  }
+  const unsigned stage_bytes = (unsigned)((nblk + N / kChunk) * S::BLK);
   ConvArgs g{};
   g.B = p.B; g.H = p.H; g.W = p.W; g.Wt = p.Wt; g.Ht = p.Ht;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kWgStages; ++s) {
+    for (int s = 0; s < NS; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
@@ -276,8 +301,8 @@ k_conv3x3_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant_
     if (lane == 0) {
       int issued = 0;
       for (int ks = 0; ks < KS; ++ks) {
-        const int s = ks % kWgStages;
-        if (ks >= kWgStages && !tc::mbar_wait(&empty[s], ((ks / kWgStages) - 1) & 1)) {
+        const int s = ks % NS;
+        if (ks >= NS && !tc::mbar_wait(&empty[s], ((ks / NS) - 1) & 1)) {
           flag_fault(p.fault);
           break;
         }
@@ -285,22 +310,25 @@ k_conv3x3_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant_
         tile_origin(g, t0 + ks, &n, &y0, &x0);
         uint8_t* st = sm + s * S::STAGE;
         tc::mbar_expect_tx(&full[s], stage_bytes);
-        for (int b = 0; b < ci_blocks; ++b)
-          tc::tma_load_4d(st + b * S::BLK, &xmap, p.in_off + mt * kTileM + b * kChunk,
-                          x0 + tap % 3 - 1, y0 + tap / 3 - 1, n, &full[s]);
+        for (int b = 0; b < 4; ++b) {
+          int tp, c0;
+          if (wg_block(p, grp, mt, b, &tp, &c0))
+            tc::tma_load_4d(st + b * S::BLK, &xmap, p.in_off + c0, x0 + tp % 3 - 1, y0 + tp / 3 - 1,
+                            n, &full[s]);
+        }
         for (int b = 0; b < N / kChunk; ++b)
           tc::tma_load_4d(st + S::A + b * S::BLK, &dmap, b * kChunk, x0, y0, n, &full[s]);
         issued = ks + 1;
       }
-      for (int ks = issued - kWgStages > 0 ? issued - kWgStages : 0; ks < issued; ++ks)
-        tc::mbar_wait(&full[ks % kWgStages], (ks / kWgStages) & 1);
+      for (int ks = issued - NS > 0 ? issued - NS : 0; ks < issued; ++ks)
+        tc::mbar_wait(&full[ks % NS], (ks / NS) & 1);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t id = tc::idesc_bf16(kTileM, N, 1, 1);
       for (int ks = 0; ks < KS; ++ks) {
-        const int s = ks % kWgStages;
-        if (!tc::mbar_wait(&full[s], (ks / kWgStages) & 1)) {
+        const int s = ks % NS;
+        if (!tc::mbar_wait(&full[s], (ks / NS) & 1)) {
           flag_fault(p.fault);
           break;
         }
@@ -317,14 +345,13 @@ k_conv3x3_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant_
       tc::mma_commit(&accf);
     }
   } else {
-    const int q = warp & 3;
-    const int row = q * 32 + lane;          // input channel within the tile
+    const int q = warp & 3;                 // accumulator rows 32 q .. 32 q + 31 = block q
     const bool ok = tc::mbar_wait(&accf, 0);
     if (!ok) flag_fault(p.fault);
     tc::fence_after_sync();
-    const int ci_tiles = (p.cin + kTileM - 1) / kTileM;
-    float* out = p.ws + ((((int64_t)split * 9 + tap) * ci_tiles + mt) * kTileM + row) * p.cout;
-    const bool live = row < ci_blocks * kChunk;
+    int tp = 0, c0 = 0;
+    const bool live = wg_block(p, grp, mt, q, &tp, &c0);
+    float* out = p.ws + ((((int64_t)split * 9 + tp) * p.cin) + c0 + lane) * p.cout;
 #pragma unroll 1
     for (int c = 0; c < N; c += 16) {
       uint32_t r[16];
@@ -350,18 +377,16 @@ k_conv3x3_wgrad(const __grid_constant__ CUtensorMap xmap, const __grid_constant_
 // dw[tap][co][ci] = sum over splits of ws[split][tap][ci][co] (fixed order).
 __global__ void k_wgrad_reduce(const float* __restrict__ ws, int splits, int cin, int cout,
                                float* __restrict__ dw, int accumulate) {
-  const int ci_tiles = (cin + kTileM - 1) / kTileM;
   const int64_t total = (int64_t)9 * cout * cin;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int ci = (int)(i % cin);
     const int co = (int)((i / cin) % cout);
     const int tap = (int)(i / ((int64_t)cin * cout));
-    const int64_t per = (int64_t)9 * ci_tiles * kTileM * cout;
-    const int64_t off = ((int64_t)tap * ci_tiles * kTileM + ci) * cout + co;
-    float s = 0.f;
-    for (int k = 0; k < splits; ++k) s += ws[k * per + off];
-    dw[i] = accumulate ? dw[i] + s : s;
+    const int64_t off = ((int64_t)tap * cin + ci) * cout + co;
+    float sum = 0.f;
+    for (int k = 0; k < splits; ++k) sum += ws[k * total + off];
+    dw[i] = accumulate ? dw[i] + sum : sum;
   }
 }
 
@@ -399,6 +424,143 @@ __global__ void k_colsum(const float* __restrict__ part, int nblk, int C, float*
   float s = 0.f;
   for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * C + c];
   out[c] = accumulate ? out[c] + s : s;
+}
+
+// ---- vectorised versions (8 bf16 or 4 fp32 channels per thread; channel
+// counts, strides and offsets multiples of 8, 16-byte aligned pointers)
+struct alignas(16) bf8 { bf16 v[8]; };
+
+__global__ void k_gelu_bwd8(int64_t npix, int C, const float* __restrict__ da, int da_stride,
+                            int da_off, const bf16* __restrict__ z, bf16* __restrict__ dz,
+                            float* __restrict__ colpart) {
+  extern __shared__ float red8[];   // blockDim.x * 8 floats
+  const int G = C / 8, ppb = (int)blockDim.x / G;
+  const int g = threadIdx.x % G, pl = threadIdx.x / G;
+  float acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+  if (pl < ppb) {
+    for (int64_t p = (int64_t)blockIdx.x * ppb + pl; p < npix; p += (int64_t)gridDim.x * ppb) {
+      const float4* ap = reinterpret_cast<const float4*>(da + p * da_stride + da_off + 8 * g);
+      const float4 a0 = ap[0], a1 = ap[1];
+      const bf8 zz = *reinterpret_cast<const bf8*>(z + p * C + 8 * g);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      bf8 out;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        out.v[j] = __float2bfloat16(av[j] * gelu_grad(__bfloat162float(zz.v[j])));
+        acc[j] += __bfloat162float(out.v[j]);
+      }
+      *reinterpret_cast<bf8*>(dz + p * C + 8 * g) = out;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red8[threadIdx.x * 8 + j] = acc[j];
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    float sum = 0.f;
+    for (int q = 0; q < ppb; ++q) sum += red8[(q * G + c / 8) * 8 + (c & 7)];
+    colpart[(int64_t)blockIdx.x * C + c] = sum;
+  }
+}
+
+// Column sums of per-block partials: one CTA per column, a fixed order.
+__global__ void k_colsum_par(const float* __restrict__ part, int nblk, int C, float* __restrict__ out,
+                             int accumulate) {
+  const int c = blockIdx.x;
+  float sum = 0.f;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) sum += part[(int64_t)b * C + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  __shared__ float wsum[32];
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    out[c] = accumulate ? out[c] + t : t;
+  }
+}
+
+__global__ void k_pool2_8(int B, int H, int W, int C, const bf16* __restrict__ x, int xs, int xo,
+                          bf16* __restrict__ y) {
+  const int h = H / 2, w = W / 2, G = C / 8;
+  const int64_t total = (int64_t)B * h * w * G;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i % G);
+    const int64_t pp = i / G;
+    const int xx = (int)(pp % w), yy = (int)((pp / w) % h);
+    const int64_t n = pp / ((int64_t)w * h);
+    const int64_t b0 = (n * H + 2 * yy) * W + 2 * xx;
+    const bf8 v0 = *reinterpret_cast<const bf8*>(x + b0 * xs + xo + 8 * g);
+    const bf8 v1 = *reinterpret_cast<const bf8*>(x + (b0 + 1) * xs + xo + 8 * g);
+    const bf8 v2 = *reinterpret_cast<const bf8*>(x + (b0 + W) * xs + xo + 8 * g);
+    const bf8 v3 = *reinterpret_cast<const bf8*>(x + (b0 + W + 1) * xs + xo + 8 * g);
+    bf8 out;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      out.v[j] = __float2bfloat16(0.25f * (__bfloat162float(v0.v[j]) + __bfloat162float(v1.v[j]) +
+                                           __bfloat162float(v2.v[j]) + __bfloat162float(v3.v[j])));
+    *reinterpret_cast<bf8*>(y + pp * C + 8 * g) = out;
+  }
+}
+
+__global__ void k_pool2_bwd4(int B, int H, int W, int C, const float* __restrict__ dy,
+                             float* __restrict__ dx, int dxs, int dxo, int accumulate) {
+  const int h = H / 2, w = W / 2, G = C / 4;
+  const int64_t total = (int64_t)B * H * W * G;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i % G);
+    const int64_t pp = i / G;
+    const int xx = (int)(pp % W), yy = (int)((pp / W) % H);
+    const int64_t n = pp / ((int64_t)W * H);
+    float4 v = *reinterpret_cast<const float4*>(dy + ((n * h + yy / 2) * w + xx / 2) * C + 4 * g);
+    v.x *= 0.25f; v.y *= 0.25f; v.z *= 0.25f; v.w *= 0.25f;
+    float4* d = reinterpret_cast<float4*>(dx + pp * dxs + dxo + 4 * g);
+    if (accumulate) {
+      const float4 o = *d;
+      v.x += o.x; v.y += o.y; v.z += o.z; v.w += o.w;
+    }
+    *d = v;
+  }
+}
+
+__global__ void k_up2_8(int B, int h, int w, int C, const bf16* __restrict__ x, bf16* __restrict__ y,
+                        int ys, int yo) {
+  const int H = 2 * h, W = 2 * w, G = C / 8;
+  const int64_t total = (int64_t)B * H * W * G;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i % G);
+    const int64_t pp = i / G;
+    const int xx = (int)(pp % W), yy = (int)((pp / W) % H);
+    const int64_t n = pp / ((int64_t)W * H);
+    *reinterpret_cast<bf8*>(y + pp * ys + yo + 8 * g) =
+        *reinterpret_cast<const bf8*>(x + ((n * h + yy / 2) * w + xx / 2) * C + 8 * g);
+  }
+}
+
+__global__ void k_up2_bwd4(int B, int h, int w, int C, const float* __restrict__ dy, int dys, int dyo,
+                           float* __restrict__ dx) {
+  const int H = 2 * h, W = 2 * w, G = C / 4;
+  const int64_t total = (int64_t)B * h * w * G;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i % G);
+    const int64_t pp = i / G;
+    const int xx = (int)(pp % w), yy = (int)((pp / w) % h);
+    const int64_t n = pp / ((int64_t)w * h);
+    const int64_t b0 = (n * H + 2 * yy) * W + 2 * xx;
+    const float4 a = *reinterpret_cast<const float4*>(dy + b0 * dys + dyo + 4 * g);
+    const float4 b = *reinterpret_cast<const float4*>(dy + (b0 + 1) * dys + dyo + 4 * g);
+    const float4 c = *reinterpret_cast<const float4*>(dy + (b0 + W) * dys + dyo + 4 * g);
+    const float4 d = *reinterpret_cast<const float4*>(dy + (b0 + W + 1) * dys + dyo + 4 * g);
+    *reinterpret_cast<float4*>(dx + pp * C + 4 * g) =
+        make_float4(a.x + b.x + c.x + d.x, a.y + b.y + c.y + d.y, a.z + b.z + c.z + d.z,
+                    a.w + b.w + c.w + d.w);
+  }
 }
 
 // Head parameter grads from the per-block partials, summed in block order.
@@ -889,8 +1051,14 @@ static unsigned* fault_word() {
 }
 
 // Pixel-tile ranges of the weight gradient: about two waves of CTAs.
-static int wgrad_splits(int tiles, int mtiles) {
-  int want = (2 * sm_count() + 9 * mtiles - 1) / (9 * mtiles);
+static void wgrad_groups(int cin, int* tpg, int* ngroups, int* mtiles) {
+  *tpg = (cin < kTileM && kTileM % cin == 0) ? kTileM / cin : 1;
+  *ngroups = (9 + *tpg - 1) / *tpg;
+  *mtiles = *tpg > 1 ? 1 : (cin + kTileM - 1) / kTileM;
+}
+
+static int wgrad_splits(int tiles, int cta_per_split) {
+  int want = (2 * sm_count() + cta_per_split - 1) / cta_per_split;
   if (want < 1) want = 1;
   if (want > tiles) want = tiles;
   return want;
@@ -936,9 +1104,10 @@ int opyx_conv3x3(const opyx_conv3x3_desc* d, void* stream) {
 size_t opyx_conv3x3_wgrad_workspace(const opyx_conv3x3_desc* d) {
   if (conv_check(d)) return 0;
   const int64_t tiles = (int64_t)d->batch * d->height * d->width / kTileM;
-  const int mtiles = (d->in_channels + kTileM - 1) / kTileM;
-  const int splits = wgrad_splits((int)tiles, mtiles);
-  return (size_t)splits * 9 * mtiles * kTileM * d->out_channels * sizeof(float);
+  int tpg, ngroups, mtiles;
+  wgrad_groups(d->in_channels, &tpg, &ngroups, &mtiles);
+  const int splits = wgrad_splits((int)tiles, ngroups * mtiles);
+  return (size_t)splits * 9 * d->in_channels * d->out_channels * sizeof(float);
 }
 
 int opyx_conv3x3_wgrad(const opyx_conv3x3_desc* d, const void* dy, float* dw, int accumulate,
@@ -952,8 +1121,9 @@ int opyx_conv3x3_wgrad(const opyx_conv3x3_desc* d, const void* dy, float* dw, in
   if ((st = tile_shape(d->height, d->width, &Wt, &Ht))) return st;
   const int64_t tiles = (int64_t)d->batch * d->height * d->width / kTileM;
   if (tiles > INT32_MAX) return OPYX_ERR_UNSUPPORTED;
-  const int mtiles = (d->in_channels + kTileM - 1) / kTileM;
-  const int splits = wgrad_splits((int)tiles, mtiles);
+  int tpg, ngroups, mtiles;
+  wgrad_groups(d->in_channels, &tpg, &ngroups, &mtiles);
+  const int splits = wgrad_splits((int)tiles, ngroups * mtiles);
   if (ws_bytes < opyx_conv3x3_wgrad_workspace(d)) return OPYX_ERR_WORKSPACE;
   CUtensorMap xm, dm;
   if ((st = act_map(&xm, d->x, d->batch, d->height, d->width, d->in_stride, Wt, Ht))) return st;
@@ -961,15 +1131,16 @@ int opyx_conv3x3_wgrad(const opyx_conv3x3_desc* d, const void* dy, float* dw, in
   WgArgs a{};
   a.B = d->batch; a.H = d->height; a.W = d->width; a.Wt = Wt; a.Ht = Ht;
   a.cin = d->in_channels; a.in_off = d->in_offset; a.cout = N;
+  a.tpg = tpg; a.ngroups = ngroups;
   a.tiles = (int)tiles;
   a.tiles_per_cta = (int)((tiles + splits - 1) / splits);
   a.ws = (float*)ws;
   a.fault = fault_word();
   cudaStream_t s = (cudaStream_t)stream;
   switch (N) {
-    case 32: st = launch_wgrad<32>(xm, dm, a, 9 * splits, mtiles, s); break;
-    case 64: st = launch_wgrad<64>(xm, dm, a, 9 * splits, mtiles, s); break;
-    default: st = launch_wgrad<128>(xm, dm, a, 9 * splits, mtiles, s); break;
+    case 32: st = launch_wgrad<32>(xm, dm, a, ngroups * splits, mtiles, s); break;
+    case 64: st = launch_wgrad<64>(xm, dm, a, ngroups * splits, mtiles, s); break;
+    default: st = launch_wgrad<128>(xm, dm, a, ngroups * splits, mtiles, s); break;
   }
   if (st) return st;
   const int64_t total = (int64_t)9 * N * d->in_channels;
@@ -999,11 +1170,17 @@ int opyx_gelu_bwd(int64_t npix, int C, const float* da, int da_stride, int da_of
   if (ws_bytes < opyx_gelu_bwd_workspace(npix, C)) return OPYX_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   const int nblk = sm_count() * 4;
-  const int threads = 256 / C * C;
-  k_gelu_bwd<<<nblk, threads, threads * sizeof(float), s>>>(npix, C, da, da_stride, da_off,
-                                                            (const bf16*)z, (bf16*)dz, (float*)ws);
+  if (C % 8 == 0 && 256 % (C / 8) == 0 && da_stride % 4 == 0 && da_off % 4 == 0 && al16(da) &&
+      al16(z) && al16(dz)) {
+    k_gelu_bwd8<<<nblk, 256, 256 * 8 * sizeof(float), s>>>(npix, C, da, da_stride, da_off,
+                                                           (const bf16*)z, (bf16*)dz, (float*)ws);
+  } else {
+    const int threads = 256 / C * C;
+    k_gelu_bwd<<<nblk, threads, threads * sizeof(float), s>>>(npix, C, da, da_stride, da_off,
+                                                              (const bf16*)z, (bf16*)dz, (float*)ws);
+  }
   OPYX_CHECK_LAUNCH();
-  k_colsum<<<(C + 127) / 128, 128, 0, s>>>((const float*)ws, nblk, C, dbias, accumulate);
+  k_colsum_par<<<C, 256, 0, s>>>((const float*)ws, nblk, C, dbias, accumulate);
   return check_launch();
 }
 
@@ -1011,8 +1188,12 @@ int opyx_pool2(int B, int H, int W, int C, const void* x, int xs, int xo, void* 
   if (B < 1 || H < 2 || W < 2 || (H | W) & 1 || C < 1 || !x || !y || xo < 0 || xo + C > xs)
     return OPYX_ERR_ARG;
   const int64_t total = (int64_t)B * (H / 2) * (W / 2) * C;
-  k_pool2<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)x, xs, xo,
-                                                                   (bf16*)y);
+  if (C % 8 == 0 && xs % 8 == 0 && xo % 8 == 0 && al16(x) && al16(y))
+    k_pool2_8<<<grid_for(total / 8, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)x,
+                                                                           xs, xo, (bf16*)y);
+  else
+    k_pool2<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)x, xs, xo,
+                                                                     (bf16*)y);
   return check_launch();
 }
 
@@ -1021,16 +1202,24 @@ int opyx_pool2_bwd(int B, int H, int W, int C, const float* dy, float* dx, int d
   if (B < 1 || H < 2 || W < 2 || (H | W) & 1 || C < 1 || !dy || !dx || dxo < 0 || dxo + C > dxs)
     return OPYX_ERR_ARG;
   const int64_t total = (int64_t)B * H * W * C;
-  k_pool2_bwd<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dy, dx, dxs, dxo,
-                                                                       accumulate);
+  if (C % 4 == 0 && dxs % 4 == 0 && dxo % 4 == 0 && al16(dy) && al16(dx))
+    k_pool2_bwd4<<<grid_for(total / 4, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dy, dx, dxs,
+                                                                               dxo, accumulate);
+  else
+    k_pool2_bwd<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dy, dx, dxs, dxo,
+                                                                         accumulate);
   return check_launch();
 }
 
 int opyx_up2(int B, int h, int w, int C, const void* x, void* y, int ys, int yo, void* stream) {
   if (B < 1 || h < 1 || w < 1 || C < 1 || !x || !y || yo < 0 || yo + C > ys) return OPYX_ERR_ARG;
   const int64_t total = (int64_t)B * 4 * h * w * C;
-  k_up2<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)x, (bf16*)y,
-                                                                ys, yo);
+  if (C % 8 == 0 && ys % 8 == 0 && yo % 8 == 0 && al16(x) && al16(y))
+    k_up2_8<<<grid_for(total / 8, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)x,
+                                                                         (bf16*)y, ys, yo);
+  else
+    k_up2<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)x, (bf16*)y,
+                                                                  ys, yo);
   return check_launch();
 }
 
@@ -1038,7 +1227,11 @@ int opyx_up2_bwd(int B, int h, int w, int C, const float* dy, int dys, int dyo, 
                  void* stream) {
   if (B < 1 || h < 1 || w < 1 || C < 1 || !dy || !dx || dyo < 0 || dyo + C > dys) return OPYX_ERR_ARG;
   const int64_t total = (int64_t)B * h * w * C;
-  k_up2_bwd<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, dy, dys, dyo, dx);
+  if (C % 4 == 0 && dys % 4 == 0 && dyo % 4 == 0 && al16(dy) && al16(dx))
+    k_up2_bwd4<<<grid_for(total / 4, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, dy, dys, dyo,
+                                                                             dx);
+  else
+    k_up2_bwd<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, dy, dys, dyo, dx);
   return check_launch();
 }
 
