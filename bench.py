@@ -349,17 +349,17 @@ def warm_start_case(a, n_eval=32):
     f, lam = instances(range(B), S)
     fd, ld = t.from_numpy(f).cuda(), t.from_numpy(lam).cuda()
     for _ in range(3):
-        net.forward(fd, ld)
+        net.forward(fd, ld, keep=False)
     e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(5):
-        net.forward(fd, ld)
+        net.forward(fd, ld, keep=False)
     e1.record()
     t.cuda.synchronize()
     fwd_s = e0.elapsed_time(e1) / 1e3 / 5
     peak = measured_peaks().get("bf16_tflops")
     layer_s, layer_fl = net.time_conv("d0", B, S)
-    res["network"] = {"batch": B, "forward_ms": round(1e3 * fwd_s, 3),
+    res["network"] = {"batch": B, "forward_ms": round(1e3 * fwd_s, 3), "mode": "inference",
                       "forward_conv_TFLOPs": round(net.conv_flops(B, S) / fwd_s / 1e12, 1),
                       "largest_layer": "d0 (64 -> 32 channels at 512^2)",
                       "layer_us": round(1e6 * layer_s, 1),

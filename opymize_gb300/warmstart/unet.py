@@ -178,9 +178,11 @@ class UNet(object):
         return d
 
     # ------------------------------------------------------------- forward
-    def forward(self, f, lam):
+    def forward(self, f, lam, keep=True):
         """f: (B, S, S) fp32 device tensor, lam: (B,) fp32 device tensor.
-        Returns the (B, S, S, 3) fp32 head output (x - f, y / lambda)."""
+        Returns the (B, S, S, 3) fp32 head output (x - f, y / lambda).
+        keep=False skips storing the pre-activations the backward needs
+        (inference: a third less traffic in the convolutions' epilogues)."""
         B, S = f.shape[0], f.shape[1]
         b = self.buffers(B, S)
         s = stream_ptr()
@@ -191,7 +193,7 @@ class UNet(object):
 
         def conv(name):
             _, src, _, _, _, _, dst, _, _, _ = LAYER[name]
-            d = self._desc(name, B, S, b[src], b[dst], b["z." + name],
+            d = self._desc(name, B, S, b[src], b[dst], b["z." + name] if keep else None,
                            bias=self.params[name + ".b"], w=self.wb[name])
             _lib.call("opyx_conv3x3", C.byref(d), s)
 
@@ -317,7 +319,7 @@ class UNet(object):
         (feasible for F* = indicator of the lambda-ball).  Returns
         (B, S, S) and (B, S, S, 2) fp32 device tensors."""
         t = torch()
-        out = self.forward(f, lam)
+        out = self.forward(f, lam, keep=False)
         b = self._bufs[next(iter(self._bufs))]
         B, S = out.shape[0], out.shape[1]
         x0 = t.empty(B, S, S, device="cuda")
