@@ -75,6 +75,12 @@ size_t opyx_reduce_workspace_size(void);
 int opyx_norms(int dtype, int64_t n, const void* x, double* out, void* ws,
                void* stream);
 
+/* out[0] = sum_i x_i y_i in FP64 (deterministic; ws as opyx_norms): the
+ * inner products of the semismooth Newton solver's CG and line search
+ * (np.einsum('i,i->', ...), opymize/solvers/semismooth_newton.py:106-116). */
+int opyx_dot(int dtype, int64_t n, const void* x, const void* y, double* out, void* ws,
+             void* stream);
+
 /* ---------------------------------------------- finite differences (diff) */
 #define OPYX_MAX_DIMS 6
 typedef struct {
@@ -232,6 +238,16 @@ int opyx_l1normsproj(int dtype, int64_t N, int M1, int M2, double lbd, int matri
                      void* x, void* stream);
 /* In-place prox of sigma*F* for F = lbd*sum_i huber_alpha(|x_i|_F):
  * x_i <- proj_{|.|_F<=lbd}(x_i / (1 + sigma*alpha/lbd)), groups of m values. */
+/* Frobenius-ball projection of N groups of M values in place, recording the
+ * map's Jacobian at x: xn (N*M) = x/|x| and s (N) = lbd/|x| outside the ball,
+ * 0 and 1 inside (L1NormsProj(jacobian=True) + L12ProjJacobian.update,
+ * opymize/operators/proj.py:206-252). */
+int opyx_l1normsproj_jac(int dtype, int64_t N, int M, double lbd, void* x, void* xn, void* s,
+                         void* stream);
+/* y (+)= s_i (x_i - <xn_i, x_i> xn_i): L12ProjJacobian applied
+ * (opymize/operators/proj.py:254-276); symmetric. */
+int opyx_l12proj_jacobian(int dtype, int64_t N, int M, const void* xn, const void* s, const void* x,
+                          void* y, int add, void* stream);
 int opyx_huber_conj_prox(int dtype, int64_t N, int m, double lbd, double alpha,
                          opyx_step sigma, void* x, void* stream);
 /* In-place projection of (x1, x2) in R^M x R onto the epigraph of

@@ -129,6 +129,9 @@ SIGNATURES = {
     "opyx_broadcast_mid": (i32, [i32, vp, i64, i64, i64, vp, i32, vp]),
     "opyx_reduce_workspace_size": (sz, []),
     "opyx_norms": (i32, [i32, i64, vp, vp, vp, vp]),
+    "opyx_dot": (i32, [i32, i64, vp, vp, vp, vp, vp]),
+    "opyx_l1normsproj_jac": (i32, [i32, i64, i32, f64, vp, vp, vp, vp]),
+    "opyx_l12proj_jacobian": (i32, [i32, i64, i32, vp, vp, vp, vp, i32, vp]),
     "opyx_gradient": (i32, [P(opyx_grid), i32, vp, i32, vp, vp, i32, vp]),
     "opyx_divergence": (i32, [P(opyx_grid), i32, vp, i32, vp, vp, i32, vp]),
     "opyx_gradient_rowlp": (i32, [P(opyx_grid), i32, vp, i32, f64, i32, vp, i32, vp]),

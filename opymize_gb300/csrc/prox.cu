@@ -103,6 +103,56 @@ __global__ void k_quadepi(int64_t N, int M, double alph, const T* __restrict__ s
 
 using namespace opyx;
 
+// Projection onto the Frobenius lbd-ball of each group of M values, in
+// place, recording the Jacobian of the map at x (L1NormsProj with
+// jacobian=True and L12ProjJacobian.update, opymize/operators/proj.py:
+// 206-226, :244-252): outside the ball n = x/|x| and s = lbd/|x|, inside
+// n = 0 and s = 1, so that J v = s (v - <n, v> n) is the identity there.
+// The arithmetic is that of norm_projection (proj.py:99-108): the
+// reciprocal norm, then two scalings.
+template <typename T>
+__global__ void k_l1proj_jac(int64_t N, int M, T lbd, T* __restrict__ x, T* __restrict__ xn,
+                             T* __restrict__ s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T* g = x + i * M;
+    T* nn = xn + i * M;
+    T sq = T(0);
+    for (int k = 0; k < M; ++k) sq += g[k] * g[k];
+    const T nrm = sqrt(sq);
+    if (nrm > lbd) {
+      const T rec = T(1) / nrm;
+      for (int k = 0; k < M; ++k) {
+        nn[k] = g[k] * rec;
+        g[k] = g[k] * rec * lbd;
+      }
+      s[i] = lbd * rec;
+    } else {
+      for (int k = 0; k < M; ++k) nn[k] = T(0);
+      s[i] = T(1);
+    }
+  }
+}
+
+// y (+)= s_i (x_i - <n_i, x_i> n_i) per group (L12ProjJacobian._call_cpu,
+// proj.py:254-276: y = n; y *= -<n, x>; y += x; y *= s).
+template <typename T>
+__global__ void k_l12_jac_apply(int64_t N, int M, const T* __restrict__ xn, const T* __restrict__ s,
+                                const T* __restrict__ x, T* __restrict__ y, int add) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T* nn = xn + i * M;
+    const T* xv = x + i * M;
+    T d = T(0);
+    for (int k = 0; k < M; ++k) d += nn[k] * xv[k];
+    const T si = s[i];
+    for (int k = 0; k < M; ++k) {
+      const T v = (nn[k] * (-d) + xv[k]) * si;
+      y[i * M + k] = add ? y[i * M + k] + v : v;
+    }
+  }
+}
+
 #define LAUNCH(kernel, n, ...)                                                  \
   do {                                                                          \
     if ((n) == 0) return OPYX_OK;                                               \
@@ -157,6 +207,18 @@ int opyx_l1normsproj(int dtype, int64_t N, int M1, int M2, double lbd, int matri
   if (matrixnorm == OPYX_NORM_SPECTRAL && M1 != 1 && M2 != 1 && M1 != 2 && M2 != 2)
     return OPYX_ERR_UNSUPPORTED;
   LAUNCH(k_l1proj, N, N, M1, M2, (T)lbd, matrixnorm == OPYX_NORM_SPECTRAL, (T*)x);
+}
+
+int opyx_l1normsproj_jac(int dtype, int64_t N, int M, double lbd, void* x, void* xn, void* s,
+                         void* stream) {
+  if (N < 0 || M < 1 || !(lbd > 0) || (N > 0 && (!x || !xn || !s))) return OPYX_ERR_ARG;
+  LAUNCH(k_l1proj_jac, N, N, M, (T)lbd, (T*)x, (T*)xn, (T*)s);
+}
+
+int opyx_l12proj_jacobian(int dtype, int64_t N, int M, const void* xn, const void* s, const void* x,
+                          void* y, int add, void* stream) {
+  if (N < 0 || M < 1 || (N > 0 && (!xn || !s || !x || !y))) return OPYX_ERR_ARG;
+  LAUNCH(k_l12_jac_apply, N, N, M, (const T*)xn, (const T*)s, (const T*)x, (T*)y, add);
 }
 
 int opyx_huber_conj_prox(int dtype, int64_t N, int m, double lbd, double alpha,

@@ -89,6 +89,19 @@ k_norms(int64_t n, const T* __restrict__ x, double* out, double* partials, unsig
   });
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+k_dot(int64_t n, const T* __restrict__ x, const T* __restrict__ y, double* out, double* partials,
+      unsigned* ticket) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)x[i] * (double)y[i];
+  double vals[1] = {s};
+  const int ops[1] = {RED_SUM};
+  block_reduce_and_finish<1>(vals, ops, partials, ticket, [&](double* tot) { out[0] = tot[0]; });
+}
+
 }  // namespace opyx
 
 using namespace opyx;
@@ -188,6 +201,18 @@ int opyx_norms(int dtype, int64_t n, const void* x, double* out, void* ws, void*
   if (g > (unsigned)kRedBlocks) g = kRedBlocks;
   OPYX_DISPATCH(dtype, T, (k_norms<T><<<g, kRedThreads, 0, (cudaStream_t)stream>>>(
                               n, (const T*)x, out, partials, ticket)));
+  return check_launch();
+}
+
+int opyx_dot(int dtype, int64_t n, const void* x, const void* y, double* out, void* ws, void* stream) {
+  if (n < 0 || !out || !ws || (n > 0 && (!x || !y))) return OPYX_ERR_ARG;
+  if (((uintptr_t)ws) & 7) return OPYX_ERR_WORKSPACE;
+  double* partials = (double*)ws;
+  unsigned* ticket = (unsigned*)((char*)ws + (size_t)kRedBlocks * 8 * sizeof(double));
+  unsigned g = grid_for(n, kRedThreads, 4);
+  if (g > (unsigned)kRedBlocks) g = kRedBlocks;
+  OPYX_DISPATCH(dtype, T, (k_dot<T><<<g, kRedThreads, 0, (cudaStream_t)stream>>>(
+                              n, (const T*)x, (const T*)y, out, partials, ticket)));
   return check_launch();
 }
 

@@ -243,6 +243,17 @@ def norms(x):
     return float(h[0]), float(h[1])
 
 
+def dot(x, y):
+    """<x, y> of two DeviceArrays of the same size and dtype, reduced in
+    FP64 on the device (deterministic); synchronises to return a float."""
+    if x.size != y.size or x.dtype != y.dtype:
+        raise ValueError("dot: size or dtype mismatch")
+    ws = Workspace.get(_lib.load().opyx_reduce_workspace_size(), key="dot")
+    out = DeviceArray.zeros((1,), np.float64)
+    _lib.call("opyx_dot", x.dcode, x.size, x.ptr, y.ptr, out.ptr, ws.ptr, stream_ptr())
+    return float(out.get()[0])
+
+
 def norm(x):
     """Euclidean norm of a DeviceArray (FP64 reduction)."""
     return float(np.sqrt(norms(x)[0]))

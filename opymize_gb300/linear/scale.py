@@ -39,8 +39,8 @@ class ScaleOp(LinOp):
     def _fvec(self, dtype):
         key = np.dtype(dtype).str
         if key not in self._fact_dev:
-            self._fact_dev[key] = DeviceArray.to_gpu(
-                np.broadcast_to(np.asarray(self.fact, dtype=np.float64), (self.x.size,)), dtype)
+            self._fact_dev[key] = DeviceArray.to_gpu(np.ascontiguousarray(
+                np.broadcast_to(np.asarray(self.fact, dtype=np.float64), (self.x.size,))), dtype)
         return self._fact_dev[key]
 
     def _call_gpu(self, x, y=None, add=False):

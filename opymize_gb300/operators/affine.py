@@ -141,3 +141,19 @@ class SSDProxOp(Operator):
         mask = self.ssd.mask_dev()
         _lib.call("opyx_ssd_prox", x.dcode, N, C, f.ptr, vol.ptr, None if mask is None else mask.ptr,
                   step_struct(self.tau, x.dtype), x.ptr, y.ptr, stream_ptr())
+        if jacobian:
+            # the map is a*(x + b*f) with a = 1/(1 + tau*vol) on masked pixels and
+            # 1 elsewhere (quad.py:45-55); its Jacobian is the ScaleOp diag(a)
+            return self._jacobian_op()
+
+    def _jacobian_op(self):
+        from opymize_gb300.linear.scale import ScaleOp
+        if getattr(self, "_jac", None) is None:
+            if not np.isscalar(self.tau):
+                raise NotImplementedError("the Jacobian needs a scalar step")
+            N, C = self.ssd.f.shape
+            tv = np.zeros((N, C))
+            msk = np.ones(N, dtype=bool) if self.ssd.mask is None else np.asarray(self.ssd.mask, bool)
+            tv[msk, :] = float(self.tau) * np.asarray(self.ssd.vol, dtype=np.float64)
+            self._jac = ScaleOp(N * C, 1.0 / (1.0 + tv.ravel()))
+        return self._jac

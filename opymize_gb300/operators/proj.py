@@ -2,7 +2,7 @@
 
 import numpy as np
 
-from opymize_gb300 import Variable, Operator, _lib
+from opymize_gb300 import Variable, Operator, LinOp, _lib
 from opymize_gb300.gpuarray import DeviceArray, stream_ptr
 from opymize_gb300.steps import step_struct
 
@@ -62,12 +62,54 @@ class L1NormsProj(Operator):
         self.y = self.x
         self.lbd = float(lbd)
         self.matrixnorm = matrixnorm
+        self._jacobian = L12ProjJacobian(self.N, self.M, self.lbd) \
+            if matrixnorm == "frobenius" else None
 
     def _call_gpu(self, x, y=None, add=False, jacobian=False):
-        assert not add and not jacobian
+        assert not add
+        assert self.matrixnorm == "frobenius" or not jacobian
         y = _inplace(x, y)
+        if jacobian:
+            # the projection and its Jacobian at x in one pass (proj.py:206-226)
+            J = self._jacobian
+            J._buffers(y.dtype)
+            _lib.call("opyx_l1normsproj_jac", y.dcode, self.N, self.M[0] * self.M[1], self.lbd,
+                      y.ptr, J.xn.ptr, J.s.ptr, stream_ptr())
+            return J
         _lib.call("opyx_l1normsproj", y.dcode, self.N, self.M[0], self.M[1], self.lbd,
                   _lib.NORM[self.matrixnorm], y.ptr, stream_ptr())
+
+
+class L12ProjJacobian(LinOp):
+    """Jacobian of the projection onto the Frobenius lbd-balls at the point
+    of the last L1NormsProj call with jacobian=True (opymize/operators/
+    proj.py:228-276): the identity on groups inside the ball, lbd/|x|
+    (v - <n, v> n) with n = x/|x| outside.  Symmetric.  The state (n and the
+    scale per group) lives on the device and is written by the projection."""
+
+    def __init__(self, N, M, lbd):
+        LinOp.__init__(self)
+        self.N, self.M = int(N), tuple(M)
+        self.x = Variable((self.N, self.M[0] * self.M[1]))
+        self.y = self.x
+        self.lbd = float(lbd)
+        self.adjoint = self
+        self.xn = self.s = None
+
+    def _buffers(self, dtype):
+        if self.xn is None or self.xn.dtype != np.dtype(dtype):
+            m = self.M[0] * self.M[1]
+            self.xn = DeviceArray.zeros((self.N * m,), dtype)
+            self.s = DeviceArray.empty((self.N,), dtype)
+            self.s.fill(1.0)
+
+    def _call_gpu(self, x, y=None, add=False):
+        self._buffers(x.dtype)
+        out = x if y is None else y
+        if y is None and add:
+            raise ValueError("in-place application with add is ambiguous")
+        _lib.call("opyx_l12proj_jacobian", x.dcode, self.N, self.M[0] * self.M[1], self.xn.ptr,
+                  self.s.ptr, x.ptr, out.ptr, int(bool(add)), stream_ptr())
 
 
 class HuberConjProj(Operator):
