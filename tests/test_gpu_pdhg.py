@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 SOLVER_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN)
                       if f.endswith(".npz") and f not in ("ops.npz", "epigraph.npz")
-                      and not f.startswith("sublabel"))
+                      and not f.startswith("sublabel") and f != "ssn.npz")
 SMALL_CASES = [c for c in SOLVER_CASES if c != "rof_gray256_adaptive"]
 
 
