@@ -269,7 +269,11 @@ def test_fused_matches_oracle_on_large_colour_problem():
                                                         ((200, 132), 1, 0.0, "const", True),
                                                         ((67, 1024), 2, 0.02, "precond", True),
                                                         ((1, 516), 4, 0.0, "precond", False),
-                                                        ((2048, 8), 3, 0.01, "const", False)])
+                                                        ((2048, 8), 3, 0.01, "const", False),
+                                                        ((517, 600), 1, 0.0, "precond", False),
+                                                        ((3, 2048), 1, 0.01, "precond", False),
+                                                        ((1, 516), 1, 0.0, "const", True),
+                                                        ((1000, 1028), 1, 0.0, "precond", True)])
 @pytest.mark.parametrize("iters", [1, 6, 7])
 def test_single_sweep_matches_two_passes_bitwise(dims, C, huber, steps, masked, iters):
     """2-D FP32 iterations as one sweep over HBM (second dual buffer y2 given)
