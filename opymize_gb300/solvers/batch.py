@@ -149,14 +149,36 @@ class BatchROF(object):
         return best[1]
 
     # ---------------------------------------------------------------- solve
-    def solve(self, maxiter=5000, init=None):
+    DEPTH = 2     # chunks queued ahead of the host's reads
+
+    def _capture(self, desc, nitems, part, n, slot):
+        """`n` iterations, the gap and the copy of the info records into
+        pinned slot `slot`, captured into one CUDA graph (on a private capture
+        stream) for the current active set."""
+        t = torch()
+        stream = t.cuda.Stream()
+        graph = t.cuda.CUDAGraph()
+        stream.wait_stream(t.cuda.current_stream())
+        with t.cuda.graph(graph, stream=stream):
+            self._iterate(desc, nitems, n)
+            self._gap(desc, nitems, part)
+            self._pinned[slot].copy_(self.records.t, non_blocking=True)
+        return graph
+
+    def solve(self, maxiter=5000, init=None, graph=True):
         """Iterate until every image passed its stop test or `maxiter`
         iterations; returns per image a dict with the reference's info keys
         and `iter`.  States: `self.state(i)` (x as an (H, W, C) array),
         `self.dual(i)` (y as (H, W, 2, C)).  `init`: optional starting
         points, a sequence of (x, y) per image (device tensors or arrays of
         N*C and N*2*C values; the reference's `continue_at`,
-        opymize/solvers/pdhg.py:254-255); zero otherwise."""
+        opymize/solvers/pdhg.py:254-255); zero otherwise.
+
+        Chunks of `granularity` iterations + gap are captured into CUDA
+        graphs per active set and queued DEPTH ahead of the host's reads:
+        the device-side stop test makes the kernels skip finished images, so
+        chunks queued past an image's stop leave it alone, and its iteration
+        count comes from its device check counter."""
         if self.rows_per_item is None:
             self.autotune()
         self._reset()
@@ -167,37 +189,68 @@ class BatchROF(object):
                     src = v if hasattr(v, "data_ptr") else t.from_numpy(
                         np.ascontiguousarray(v, dtype=np.float32))
                     arr[key].t.copy_(src.reshape(-1))
+        t = torch()
         names = _lib.ROF_INFO_FIELDS
+        nrec = self.rec_bytes // 8
         i_done, i_fault = names.index("done"), names.index("fault")
+        i_checks = names.index("checks")
+        off = 256 // 8
+        self._pinned = [t.empty(self.records.t.shape, dtype=self.records.t.dtype,
+                                pin_memory=True) for _ in range(self.DEPTH)]
         active = np.ones(self.n, np.uint8)
-        iters = np.zeros(self.n, np.int64)
-        last = None
         desc, nitems, part = self._describe(active, self.rows_per_item)
         self._init(desc)
+        gran = self.gran
+        graphs = None
         t0 = time.perf_counter()
-        it = 0
-        while it < maxiter and active.any():
-            n = min(self.gran, maxiter - it)
-            n += n & 1
-            self._iterate(desc, nitems, n)
-            it += n
-            self._gap(desc, nitems, part)
-            last = self._records()
+        launched = 0          # iterations queued
+        pending = []          # (slot, event, iterations after the chunk)
+        chunks = 0
+        last = None
+        while True:
+            while len(pending) < self.DEPTH and launched < maxiter and active.any():
+                n = min(gran, maxiter - launched)
+                n += n & 1
+                slot = chunks % self.DEPTH
+                if graph and n == gran:
+                    if graphs is None:
+                        graphs = [self._capture(desc, nitems, part, gran, k)
+                                  for k in range(self.DEPTH)]
+                    graphs[slot].replay()
+                    self.launches += n * self._classes + 2
+                else:
+                    self._iterate(desc, nitems, n)
+                    self._gap(desc, nitems, part)
+                    self._pinned[slot].copy_(self.records.t, non_blocking=True)
+                ev = t.cuda.Event()
+                ev.record()
+                launched += n
+                pending.append((slot, ev, launched))
+                chunks += 1
+            if not pending:
+                break
+            slot, ev, it = pending.pop(0)
+            ev.synchronize()
+            last = self._pinned[slot].numpy().reshape(self.n, nrec)[:, off:off + len(names)].copy()
             if (last[:, i_fault] != 0).any():
                 raise _lib.OpyxError("batched PDHG iteration", _lib.OPYX_ERR_LAUNCH,
                                      "a kernel gave up waiting for its own copies")
-            iters[active != 0] = it
             done = (last[:, i_done] != 0) & (active != 0)
             if done.any():
                 active[done] = 0
                 if active.any():
+                    # chunks already queued keep the old active set (finished
+                    # images are skipped on the device); new ones use the new one
                     desc, nitems, part = self._describe(active, self.rows_per_item)
+                    graphs = None
+        t.cuda.synchronize()
         self.elapsed = time.perf_counter() - t0
+        final = self.records.get().reshape(self.n, nrec)[:, off:off + len(names)]
         self.info = []
         for i in range(self.n):
-            d = {k: float(last[i, names.index(k)]) for k in INFO_KEYS}
-            d["iter"] = int(iters[i])
-            d["converged"] = bool(last[i, i_done] != 0)
+            d = {k: float(final[i, names.index(k)]) for k in INFO_KEYS}
+            d["iter"] = int(min(maxiter, round(final[i, i_checks]) * gran))
+            d["converged"] = bool(final[i, i_done] != 0)
             self.info.append(d)
         return self.info
 
