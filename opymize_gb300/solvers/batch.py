@@ -32,13 +32,19 @@ class BatchROF(object):
 
     ROWS_CANDIDATES = (8, 16, 32, 64)
 
+    GRAN_RANGE = (10, 100)
+    GRAN_PRIOR_ITERS = 1000   # iterations an instance is assumed to need when tuning the interval
+
     def __init__(self, images, lbd, huber=0.0, tol=1e-4, granularity=10, rows_per_item=None):
         if not images:
             raise ValueError("empty batch")
         self.n = len(images)
         lbds = np.broadcast_to(np.asarray(lbd, dtype=np.float64), (self.n,))
         self.tol = float(tol)
-        self.gran = int(granularity) + (int(granularity) & 1)   # iterations run in pairs
+        # granularity=None: the interval between stop tests is tuned with the rows per item
+        self.gran_auto = granularity is None
+        g = 10 if granularity is None else int(granularity)
+        self.gran = g + (g & 1)   # iterations run in pairs
         self.rows_per_item = rows_per_item
         lib = _lib.load()
         self.problems = (_lib.opyx_rof_problem * self.n)()
@@ -127,12 +133,16 @@ class BatchROF(object):
     def autotune(self, iters=4):
         """Rows per work item: each candidate runs `iters` iterations from the
         zero start, timed with CUDA events; the fastest is kept and the state
-        reset (the tuning iterations do not count)."""
+        reset (the tuning iterations do not count).  With granularity=None
+        the interval g between stop tests is chosen too: a test costs t_gap
+        and an instance runs on average g/2 iterations past its stop, so g
+        minimises t_gap/g + t_iter g/(2 n) for n = GRAN_PRIOR_ITERS, i.e.
+        g = sqrt(2 n t_gap / t_iter), even, within GRAN_RANGE."""
         t = torch()
         best = None
         active = np.ones(self.n, np.uint8)
         for rows in self.ROWS_CANDIDATES:
-            desc, nitems, _ = self._describe(active, rows)
+            desc, nitems, part = self._describe(active, rows)
             self._init(desc)
             self._iterate(desc, nitems, 2)            # warm
             e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
@@ -142,9 +152,24 @@ class BatchROF(object):
             t.cuda.synchronize()
             ms = e0.elapsed_time(e1)
             if best is None or ms < best[0]:
-                best = (ms, rows)
+                best = (ms, rows, desc, nitems, part)
         self.rows_per_item = best[1]
         self.tuning = {"rows_per_item": best[1], "ms_per_iteration": best[0] / iters}
+        if self.gran_auto:
+            _, _, desc, nitems, part = best
+            self._gap(desc, nitems, part)             # warm
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                self._gap(desc, nitems, part)
+            e1.record()
+            t.cuda.synchronize()
+            t_gap = e0.elapsed_time(e1) / 3
+            t_it = best[0] / iters
+            g = int(round(np.sqrt(2.0 * self.GRAN_PRIOR_ITERS * t_gap / max(t_it, 1e-9))))
+            g = int(np.clip(g + (g & 1), *self.GRAN_RANGE))
+            self.gran = g
+            self.tuning.update(ms_per_gap=t_gap, granularity=g)
         self._reset()
         return best[1]
 
