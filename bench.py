@@ -347,6 +347,19 @@ def warm_start_case(a, n_eval=32):
             "net_ms": round(1e3 * ev["net_s"], 2),
             "time_ratio_cold_over_warm": round(ev["speedup"], 3),
             "converged": [ev["converged_cold"], ev["converged_warm"]]}
+    # restart mode: the network corrects the iterate after 100 plain iterations
+    from opymize_gb300.warmstart import evaluate_restart
+    rnet = UNet.load(os.path.join(ROOT, "opymize_gb300", "warmstart", "unet512_restart.npz"))
+    ev = evaluate_restart(rnet, seeds, 100, S=512, tol=1e-4)
+    res["restart_after_100_relgap_0.0001"] = {
+        "iters_cold_mean": float(np.mean(ev["iters_cold"])),
+        "iters_warm_mean": float(np.mean(ev["iters_warm"])),
+        "solve_cold_ms": round(1e3 * ev["solve_cold_s"], 2),
+        "solve_warm_ms": round(1e3 * ev["solve_warm_s"], 2),
+        "net_ms": round(1e3 * ev["net_s"], 2),
+        "time_ratio_cold_over_warm": round(ev["speedup"], 3),
+        "converged": [ev["converged_cold"], ev["converged_warm"]]}
+    del rnet
     # the metric's own form: one 512^2 image at a time through the public
     # fused PDHG, zero start vs the network's proposal (continue_at), time to
     # relgap 1e-4 including the network's inference for that image

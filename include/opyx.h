@@ -527,6 +527,10 @@ int opyx_up2_bwd(int B, int h, int w, int C, const float* dy, int dys, int dyo, 
 /* Input channels: f, lambda * lam_scale (per image), zeros up to 32 (bf16). */
 int opyx_pack_input(int B, int64_t hw, const float* f, const float* lam, double lam_scale, void* x,
                     void* stream);
+/* Input of the restart mode: f, lambda * lam_scale, xb - f, yb / lambda
+ * (2 channels), zeros up to 32 (xb, yb: the current PDHG iterate). */
+int opyx_pack_input_state(int B, int64_t hw, const float* f, const float* lam, double lam_scale,
+                          const float* xb, const float* yb, void* x, void* stream);
 /* 1x1 head to K = 3 outputs (fp32) and its backward. */
 int opyx_head(int64_t npix, int K, const void* a, const float* w, const float* b, float* out,
               void* stream);
@@ -548,6 +552,10 @@ int opyx_warm_loss(int B, int H, int W, const float* out, const float* tgt, cons
 /* Proposal from head outputs: x0 = f + o0, y0 = lambda * o12 / max(1, |o12|). */
 int opyx_warm_unpack(int B, int64_t hw, const float* f, const float* lam, const float* out, float* x0,
                      float* y0, void* stream);
+/* Correction of an iterate (xb, yb): x0 = xb + o0, y0 = lambda * o12' / max(1, |o12'|)
+ * with o12' = yb / lambda + o12. */
+int opyx_warm_unpack_rel(int B, int64_t hw, const float* xb, const float* yb, const float* lam,
+                         const float* out, float* x0, float* y0, void* stream);
 /* Adam step on fp32 weights; wb / wt (optional): bf16 copy, and the
  * tap-flipped [9][in][out] copy for input-gradient convolutions. */
 int opyx_adam(int64_t n, float* w, const float* g, float* m, float* v, double lr, double b1, double b2,

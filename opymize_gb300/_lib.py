@@ -187,6 +187,8 @@ SIGNATURES = {
     "opyx_up2": (i32, [i32, i32, i32, i32, vp, vp, i32, i32, vp]),
     "opyx_up2_bwd": (i32, [i32, i32, i32, i32, vp, i32, i32, vp, vp]),
     "opyx_pack_input": (i32, [i32, i64, vp, vp, f64, vp, vp]),
+    "opyx_pack_input_state": (i32, [i32, i64, vp, vp, f64, vp, vp, vp, vp]),
+    "opyx_warm_unpack_rel": (i32, [i32, i64, vp, vp, vp, vp, vp, vp, vp]),
     "opyx_head": (i32, [i64, i32, vp, vp, vp, vp, vp]),
     "opyx_head_bwd_workspace": (sz, [i64, i32]),
     "opyx_head_bwd": (i32, [i64, i32, vp, vp, vp, vp, vp, vp, vp, sz, vp]),

@@ -658,6 +658,28 @@ __global__ void k_pack_input(int B, int64_t hw, const float* __restrict__ f,
   }
 }
 
+// Network input of the restart mode: f, lambda * lam_scale, the current
+// iterate as x - f and y / lambda (2 channels), zeros up to 32.
+__global__ void k_pack_input_state(int B, int64_t hw, const float* __restrict__ f,
+                                   const float* __restrict__ lam, float lam_scale,
+                                   const float* __restrict__ xb, const float* __restrict__ yb,
+                                   bf16* __restrict__ x) {
+  const int64_t total = (int64_t)B * hw * 32;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i & 31);
+    const int64_t pp = i >> 5;
+    const float l = lam[pp / hw];
+    float v = 0.f;
+    if (c == 0) v = f[pp];
+    else if (c == 1) v = l * lam_scale;
+    else if (c == 2) v = xb[pp] - f[pp];
+    else if (c == 3) v = yb[2 * pp] / l;
+    else if (c == 4) v = yb[2 * pp + 1] / l;
+    x[i] = __float2bfloat16(v);
+  }
+}
+
 // Head: 1x1 convolution of the last 32-channel activation to K outputs (fp32).
 template <int K>
 __global__ void k_head(int64_t npix, const bf16* __restrict__ a, const float* __restrict__ w,
@@ -893,6 +915,24 @@ __global__ void k_warm_unpack(int64_t npix, int64_t hw, const float* __restrict_
     const float l = lam[i / hw];
     x0[i] = f[i] + out[3 * i];
     const float u0 = out[3 * i + 1], u1 = out[3 * i + 2];
+    const float n = sqrtf(u0 * u0 + u1 * u1);
+    const float s = l / (n > 1.f ? n : 1.f);
+    y0[2 * i] = s * u0;
+    y0[2 * i + 1] = s * u1;
+  }
+}
+
+// Correction of a PDHG iterate: x0 = xb + o0, y0 = lambda * proj(yb / lambda + o12)
+// onto the unit ball (xb (n), yb (n, 2) the iterate the network saw).
+__global__ void k_warm_unpack_rel(int64_t npix, int64_t hw, const float* __restrict__ xb,
+                                  const float* __restrict__ yb, const float* __restrict__ lam,
+                                  const float* __restrict__ out, float* __restrict__ x0,
+                                  float* __restrict__ y0) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float l = lam[i / hw];
+    x0[i] = xb[i] + out[3 * i];
+    const float u0 = yb[2 * i] / l + out[3 * i + 1], u1 = yb[2 * i + 1] / l + out[3 * i + 2];
     const float n = sqrtf(u0 * u0 + u1 * u1);
     const float s = l / (n > 1.f ? n : 1.f);
     y0[2 * i] = s * u0;
@@ -1244,6 +1284,15 @@ int opyx_pack_input(int B, int64_t hw, const float* f, const float* lam, double 
   return check_launch();
 }
 
+int opyx_pack_input_state(int B, int64_t hw, const float* f, const float* lam, double lam_scale,
+                          const float* xb, const float* yb, void* x, void* stream) {
+  if (B < 1 || hw < 1 || !f || !lam || !xb || !yb || !x || !al16(x)) return OPYX_ERR_ARG;
+  const int64_t total = (int64_t)B * hw * 32;
+  k_pack_input_state<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(
+      B, hw, f, lam, (float)lam_scale, xb, yb, (bf16*)x);
+  return check_launch();
+}
+
 int opyx_head(int64_t npix, int K, const void* a, const float* w, const float* b, float* out,
               void* stream) {
   if (npix < 1 || K != 3 || !a || !w || !b || !out || !al16(a)) return OPYX_ERR_ARG;
@@ -1306,6 +1355,14 @@ int opyx_warm_unpack(int B, int64_t hw, const float* f, const float* lam, const 
   if (B < 1 || hw < 1 || !f || !lam || !out || !x0 || !y0) return OPYX_ERR_ARG;
   const int64_t n = (int64_t)B * hw;
   k_warm_unpack<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, hw, f, lam, out, x0, y0);
+  return check_launch();
+}
+
+int opyx_warm_unpack_rel(int B, int64_t hw, const float* xb, const float* yb, const float* lam,
+                         const float* out, float* x0, float* y0, void* stream) {
+  if (B < 1 || hw < 1 || !xb || !yb || !lam || !out || !x0 || !y0) return OPYX_ERR_ARG;
+  const int64_t n = (int64_t)B * hw;
+  k_warm_unpack_rel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, hw, xb, yb, lam, out, x0, y0);
   return check_launch();
 }
 

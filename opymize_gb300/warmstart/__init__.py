@@ -3,7 +3,7 @@ cores proposes (x0, y0), the fused PDHG finishes to the requested gap."""
 
 from opymize_gb300.warmstart.unet import UNet
 from opymize_gb300.warmstart.train import (instance, instances, make_dataset, train, predict,
-                                           evaluate, solve_batch)
+                                           evaluate, evaluate_restart, solve_batch)
 
 __all__ = ["UNet", "instance", "instances", "make_dataset", "train", "predict", "evaluate",
-           "solve_batch"]
+           "evaluate_restart", "solve_batch"]

@@ -12,7 +12,7 @@ import time
 
 import numpy as np
 
-from opymize_gb300.warmstart import UNet, make_dataset, train, evaluate
+from opymize_gb300.warmstart import UNet, make_dataset, train, evaluate, evaluate_restart
 
 EVAL_SEED0 = 10 ** 6     # held-out seeds start here; training seeds are 0 .. n-1
 
@@ -30,12 +30,14 @@ def main(argv=None):
     ap.add_argument("--eval-tols", default="1e-4", help="comma-separated relative gaps")
     ap.add_argument("--init", default=None, help="start from these weights")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--restart", type=int, default=0,
+                    help="restart mode: correct the iterate after this many plain iterations")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run this many training steps on --batch seeded images (for profilers)")
     a = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)
     t0 = time.perf_counter()
-    net = UNet.load(a.init) if a.init else UNet(seed=0)
+    net = UNet.load(a.init) if a.init else UNet(seed=0, restart=a.restart > 0)
     res = dict(size=a.size, params=net.nparams())
     if a.profile_steps > 0:
         import torch
@@ -54,7 +56,8 @@ def main(argv=None):
         print(json.dumps(res))
         return
     if a.train > 0:
-        data = make_dataset(range(a.train), S=a.size, tol=a.data_tol, maxiter=a.data_maxiter)
+        data = make_dataset(range(a.train), S=a.size, tol=a.data_tol, maxiter=a.data_maxiter,
+                            restart=a.restart)
         its = np.array([d["iter"] for d in data["infos"]])
         res.update(train_n=a.train, data_tol=a.data_tol, data_converged=int(sum(d["converged"] for d in data["infos"])),
                    data_iters_median=float(np.median(its)), data_s=time.perf_counter() - t0)
@@ -69,8 +72,11 @@ def main(argv=None):
     if a.eval > 0:
         res["eval"] = {}
         for tol in (float(v) for v in a.eval_tols.split(",")):
-            ev = evaluate(net, range(EVAL_SEED0, EVAL_SEED0 + a.eval), S=a.size, tol=tol,
-                          batch=a.batch)
+            seeds = range(EVAL_SEED0, EVAL_SEED0 + a.eval)
+            if net.restart:
+                ev = evaluate_restart(net, seeds, a.restart, S=a.size, tol=tol, batch=a.batch)
+            else:
+                ev = evaluate(net, seeds, S=a.size, tol=tol, batch=a.batch)
             r = {k: v for k, v in ev.items() if not isinstance(v, list)}
             r.update(n=a.eval, iters_cold_mean=float(np.mean(ev["iters_cold"])),
                      iters_warm_mean=float(np.mean(ev["iters_warm"])),

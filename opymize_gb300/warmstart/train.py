@@ -64,18 +64,30 @@ def solve_batch(f, lam, tol, maxiter, init=None, chunk=256, granularity=10):
     return xs, ys, infos, elapsed
 
 
-def make_dataset(seeds, S=512, tol=1e-5, maxiter=8000, chunk=256):
+def make_dataset(seeds, S=512, tol=1e-5, maxiter=8000, chunk=256, restart=0):
     """Device tensors f (n, S, S), lam (n,), target (n, S, S, 3) and the
-    solver infos for the given seeds."""
+    solver infos for the given seeds.  restart=K: the inputs also hold the
+    iterate after K plain iterations from zero ("state") and the targets are
+    the corrections (x* - x_K, (y* - y_K) / lambda) of that iterate."""
     t = torch()
     f, lam = instances(seeds, S)
-    xs, ys, infos, _ = solve_batch(f, lam, tol, maxiter, chunk=chunk)
     fd = t.from_numpy(f).cuda()
     ld = t.from_numpy(lam).cuda()
-    tgt = t.empty(len(seeds), S, S, 3, device="cuda")
-    tgt[..., 0] = xs - fd
-    tgt[..., 1:] = ys / ld.view(-1, 1, 1, 1)
-    return dict(f=fd, lam=ld, target=tgt, infos=infos)
+    n = len(seeds)
+    state = None
+    if restart:
+        xk, yk, _, _ = solve_batch(f, lam, 1e-300, restart, chunk=chunk)
+        xs, ys, infos, _ = solve_batch(f, lam, tol, maxiter, chunk=chunk,
+                                       init=(xk.view(n, -1), yk.view(n, -1)))
+        state = (xk, yk)
+        base_x, base_y = xk, yk
+    else:
+        xs, ys, infos, _ = solve_batch(f, lam, tol, maxiter, chunk=chunk)
+        base_x, base_y = fd, t.zeros_like(ys)
+    tgt = t.empty(n, S, S, 3, device="cuda")
+    tgt[..., 0] = xs - base_x
+    tgt[..., 1:] = (ys - base_y) / ld.view(-1, 1, 1, 1)
+    return dict(f=fd, lam=ld, target=tgt, infos=infos, state=state)
 
 
 def train(net, data, epochs=4, batch=32, lr=1e-3, seed=0, log=None, cosine=True):
@@ -96,9 +108,12 @@ def train(net, data, epochs=4, batch=32, lr=1e-3, seed=0, log=None, cosine=True)
             f = data["f"].index_select(0, idx)
             lam = data["lam"].index_select(0, idx)
             tgt = data["target"].index_select(0, idx)
+            st = None
+            if data.get("state") is not None:
+                st = (data["state"][0].index_select(0, idx), data["state"][1].index_select(0, idx))
             t.cuda.synchronize()
             t0 = time.perf_counter()
-            net.forward(f, lam)
+            net.forward(f, lam, state=st)
             loss = net.loss_warm(tgt)
             net.backward()
             # cosine decay of the learning rate over the run
@@ -116,19 +131,24 @@ def train(net, data, epochs=4, batch=32, lr=1e-3, seed=0, log=None, cosine=True)
     return losses, float(np.median(step_ms)) if step_ms else None
 
 
-def predict(net, f, lam, batch=32):
-    """Network proposals for device tensors f (n, S, S), lam (n,)."""
+def predict(net, f, lam, batch=32, state=None):
+    """Network proposals for device tensors f (n, S, S), lam (n,) (and, in
+    the restart mode, the iterates state = (x (n, S, S), y (n, S, S, 2)))."""
     t = torch()
     n, S = f.shape[0], f.shape[1]
     x0 = t.empty(n, S, S, device="cuda")
     y0 = t.empty(n, S, S, 2, device="cuda")
+
+    def pad(v, b0, b1):
+        v = v[b0:b1].contiguous()
+        if b1 - b0 < batch:   # keep one buffer shape: pad the last batch
+            v = t.cat([v, v[:1].expand((batch - (b1 - b0),) + tuple(v.shape[1:]))])
+        return v
+
     for b0 in range(0, n, batch):
         b1 = min(n, b0 + batch)
-        fb, lb = f[b0:b1].contiguous(), lam[b0:b1].contiguous()
-        if b1 - b0 < batch:   # keep one buffer shape: pad the last batch
-            fb = t.cat([fb, fb[:1].expand(batch - (b1 - b0), S, S)])
-            lb = t.cat([lb, lb[:1].expand(batch - (b1 - b0))])
-        xb, yb = net.predict(fb, lb)
+        st = None if state is None else (pad(state[0], b0, b1), pad(state[1], b0, b1))
+        xb, yb = net.predict(pad(f, b0, b1), pad(lam, b0, b1), state=st)
         x0[b0:b1] = xb[:b1 - b0]
         y0[b0:b1] = yb[:b1 - b0]
     return x0, y0
@@ -140,6 +160,8 @@ def evaluate(net, seeds, S=512, tol=1e-4, maxiter=20000, batch=32):
     t = torch()
     f, lam = instances(seeds, S)
     fd, ld = t.from_numpy(f).cuda(), t.from_numpy(lam).cuda()
+    if getattr(net, "restart", False):
+        raise ValueError("use evaluate_restart for a restart-mode network")
     _, _, cold, t_cold = solve_batch(f, lam, tol, maxiter)
     t.cuda.synchronize()
     t0 = time.perf_counter()
@@ -150,10 +172,39 @@ def evaluate(net, seeds, S=512, tol=1e-4, maxiter=20000, batch=32):
     _, _, warm, t_warm = solve_batch(f, lam, tol, maxiter, init=(x0.view(n, -1), y0.view(n, -1)))
     it_c = np.array([d["iter"] for d in cold])
     it_w = np.array([d["iter"] for d in warm])
+
     return dict(seeds=list(seeds), iters_cold=it_c.tolist(), iters_warm=it_w.tolist(),
                 relgap_cold=[d["relgap"] for d in cold], relgap_warm=[d["relgap"] for d in warm],
                 converged_cold=int(sum(d["converged"] for d in cold)),
                 converged_warm=int(sum(d["converged"] for d in warm)),
                 solve_cold_s=t_cold, solve_warm_s=t_warm, net_s=t_net,
                 speedup=t_cold / (t_warm + t_net),
+                mean_iter_ratio=float(it_c.mean() / max(1.0, it_w.mean())))
+
+
+def evaluate_restart(net, seeds, K, S=512, tol=1e-4, maxiter=20000, batch=32):
+    """The restart mode on held-out seeds: K plain iterations from zero (the
+    stop test active), the network's correction of that iterate, then PDHG
+    to the same stop test; against the plain solve from zero.  Iterations
+    and times include the first K (or fewer) iterations and the network."""
+    t = torch()
+    f, lam = instances(seeds, S)
+    fd, ld = t.from_numpy(f).cuda(), t.from_numpy(lam).cuda()
+    n = len(seeds)
+    _, _, cold, t_cold = solve_batch(f, lam, tol, maxiter)
+    xk, yk, first, t_first = solve_batch(f, lam, tol, K)
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    x0, y0 = predict(net, fd, ld, batch=batch, state=(xk, yk))
+    t.cuda.synchronize()
+    t_net = time.perf_counter() - t0
+    _, _, rest, t_rest = solve_batch(f, lam, tol, maxiter, init=(x0.view(n, -1), y0.view(n, -1)))
+    it_c = np.array([d["iter"] for d in cold])
+    it_w = np.array([d["iter"] for d in first]) + np.array([d["iter"] for d in rest])
+    return dict(seeds=list(seeds), K=K, iters_cold=it_c.tolist(), iters_warm=it_w.tolist(),
+                relgap_cold=[d["relgap"] for d in cold], relgap_warm=[d["relgap"] for d in rest],
+                converged_cold=int(sum(d["converged"] for d in cold)),
+                converged_warm=int(sum(d["converged"] for d in rest)),
+                solve_cold_s=t_cold, solve_warm_s=t_first + t_rest, net_s=t_net,
+                speedup=t_cold / (t_first + t_rest + t_net),
                 mean_iter_ratio=float(it_c.mean() / max(1.0, it_w.mean())))

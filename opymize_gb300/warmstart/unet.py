@@ -64,15 +64,20 @@ class UNet(object):
     per-shape activation buffers.  `forward` / `backward` / `adam_step` run
     one training step; `predict` proposes (x0, y0) for a batch of images."""
 
-    def __init__(self, seed=0):
+    def __init__(self, seed=0, restart=False):
+        """restart=False: proposals from (f, lambda) alone.  restart=True:
+        corrections of a PDHG iterate (x, y), which is fed as three more
+        input channels (x - f, y / lambda)."""
         t = torch()
         g = t.Generator(device="cpu").manual_seed(seed)
+        self.restart = bool(restart)
+        self.nin = 5 if self.restart else 2          # input channels in use
         self.params = {}
         for name, _, _, _, cin, cout, _, _, _, _ in LAYERS:
             # He initialisation for GELU layers
             w = t.randn(9, cout, cin, generator=g) * np.sqrt(2.0 / (9 * cin))
             if name == "e0a":
-                w[:, :, 2:] = 0.0            # the padding input channels stay zero
+                w[:, :, self.nin:] = 0.0     # the padding input channels stay zero
             self.params[name + ".w"] = w
             self.params[name + ".b"] = t.zeros(cout)
         self.params["head.w"] = t.randn(HEAD_K, 32, generator=g) * np.sqrt(1.0 / 32) * 0.1
@@ -98,8 +103,8 @@ class UNet(object):
                       _p(self.wb[name]), _p(self.wt[name]), stream_ptr())
 
     def nparams(self):
-        """Trainable parameters (e0a's 30 zero input channels excluded)."""
-        return sum(v.numel() for v in self.params.values()) - 9 * 32 * 30
+        """Trainable parameters (e0a's zero padding input channels excluded)."""
+        return sum(v.numel() for v in self.params.values()) - 9 * 32 * (32 - self.nin)
 
     def buffers(self, B, S):
         key = (B, S)
@@ -122,7 +127,9 @@ class UNet(object):
                  p1=act(2, 64), a2a=act(2, 128), cat2=act(2, 256), ad2=act(2, 64),
                  p2=act(3, 128), a3=act(3, 128),
                  out=t.empty(B, S, S, HEAD_K, device="cuda"),
-                 f=t.empty(B, S, S, device="cuda"), lam=t.empty(B, device="cuda"))
+                 f=t.empty(B, S, S, device="cuda"), lam=t.empty(B, device="cuda"),
+                 xb=t.empty(B, S, S, device="cuda") if self.restart else None,
+                 yb=t.empty(B, S, S, 2, device="cuda") if self.restart else None)
         for name, _, _, _, _, cout, _, _, _, lev in LAYERS:
             b["z." + name] = act(lev, cout)
         self._bufs = {key: b}
@@ -178,18 +185,28 @@ class UNet(object):
         return d
 
     # ------------------------------------------------------------- forward
-    def forward(self, f, lam, keep=True):
-        """f: (B, S, S) fp32 device tensor, lam: (B,) fp32 device tensor.
-        Returns the (B, S, S, 3) fp32 head output (x - f, y / lambda).
-        keep=False skips storing the pre-activations the backward needs
-        (inference: a third less traffic in the convolutions' epilogues)."""
+    def forward(self, f, lam, keep=True, state=None):
+        """f: (B, S, S) fp32 device tensor, lam: (B,) fp32 device tensor,
+        state: the restart mode's iterate (x (B, S, S), y (B, S, S, 2)).
+        Returns the (B, S, S, 3) fp32 head output: (x - f, y / lambda), or in
+        the restart mode the corrections of (x, y / lambda).  keep=False
+        skips storing the pre-activations the backward needs (inference: a
+        third less traffic in the convolutions' epilogues)."""
         B, S = f.shape[0], f.shape[1]
         b = self.buffers(B, S)
         s = stream_ptr()
         if f.data_ptr() != b["f"].data_ptr():
             b["f"].copy_(f)
             b["lam"].copy_(lam)
-        _lib.call("opyx_pack_input", B, S * S, _p(b["f"]), _p(b["lam"]), LAM_SCALE, _p(b["in0"]), s)
+        if self.restart:
+            if state is None:
+                raise ValueError("the restart mode needs the current iterate")
+            b["xb"].copy_(state[0].reshape(B, S, S))
+            b["yb"].copy_(state[1].reshape(B, S, S, 2))
+            _lib.call("opyx_pack_input_state", B, S * S, _p(b["f"]), _p(b["lam"]), LAM_SCALE,
+                      _p(b["xb"]), _p(b["yb"]), _p(b["in0"]), s)
+        else:
+            _lib.call("opyx_pack_input", B, S * S, _p(b["f"]), _p(b["lam"]), LAM_SCALE, _p(b["in0"]), s)
 
         def conv(name):
             _, src, _, _, _, _, dst, _, _, _ = LAYER[name]
@@ -296,7 +313,7 @@ class UNet(object):
     def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         self.steps += 1
         s = stream_ptr()
-        self.grads["e0a.w"].view(9, 32, 32)[:, :, 2:] = 0.0
+        self.grads["e0a.w"].view(9, 32, 32)[:, :, self.nin:] = 0.0
         for k, w in self.params.items():
             name = k.split(".")[0]
             conv = k.endswith(".w") and name in LAYER
@@ -313,19 +330,24 @@ class UNet(object):
                                  "a convolution gave up waiting for its own copies")
 
     # ------------------------------------------------------------- inference
-    def predict(self, f, lam):
+    def predict(self, f, lam, state=None):
         """(x0, y0) for images f (B, S, S) and lambdas (B,) (device tensors):
         x0 = f + out0, y0 = lambda * out[1:3] projected onto the unit ball
-        (feasible for F* = indicator of the lambda-ball).  Returns
-        (B, S, S) and (B, S, S, 2) fp32 device tensors."""
+        (feasible for F* = indicator of the lambda-ball); in the restart mode
+        the corrected iterate (x + out0, lambda * proj(y / lambda + out[1:3])).
+        Returns (B, S, S) and (B, S, S, 2) fp32 device tensors."""
         t = torch()
-        out = self.forward(f, lam, keep=False)
+        out = self.forward(f, lam, keep=False, state=state)
         b = self._bufs[next(iter(self._bufs))]
         B, S = out.shape[0], out.shape[1]
         x0 = t.empty(B, S, S, device="cuda")
         y0 = t.empty(B, S, S, 2, device="cuda")
-        _lib.call("opyx_warm_unpack", B, S * S, _p(b["f"]), _p(b["lam"]), _p(out), _p(x0), _p(y0),
-                  stream_ptr())
+        if self.restart:
+            _lib.call("opyx_warm_unpack_rel", B, S * S, _p(b["xb"]), _p(b["yb"]), _p(b["lam"]),
+                      _p(out), _p(x0), _p(y0), stream_ptr())
+        else:
+            _lib.call("opyx_warm_unpack", B, S * S, _p(b["f"]), _p(b["lam"]), _p(out), _p(x0),
+                      _p(y0), stream_ptr())
         return x0, y0
 
     # ------------------------------------------------------------ measurement
@@ -361,7 +383,9 @@ class UNet(object):
 
     # -------------------------------------------------------------- storage
     def state_dict(self):
-        return {k: v.detach().cpu().numpy() for k, v in self.params.items()}
+        d = {k: v.detach().cpu().numpy() for k, v in self.params.items()}
+        d["restart"] = np.array(int(self.restart))
+        return d
 
     def load_state_dict(self, sd):
         t = torch()
@@ -374,7 +398,8 @@ class UNet(object):
 
     @classmethod
     def load(cls, path):
-        net = cls()
         with np.load(path) as d:
-            net.load_state_dict({k: d[k] for k in d.files})
+            sd = {k: d[k] for k in d.files}
+        net = cls(restart=bool(int(sd.pop("restart", 0))))
+        net.load_state_dict(sd)
         return net

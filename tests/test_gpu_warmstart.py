@@ -165,3 +165,19 @@ def test_warm_loss_matches_torch_autograd():
               w[3], grad.data_ptr(), scr.data_ptr(), parts.data_ptr(), 64, None)
     assert abs(parts.sum().item() - L.item()) <= 1e-5 * L.item()
     assert rel(grad.cpu().double().numpy(), o.grad.numpy()) < 1e-5
+
+
+def test_restart_mode_beats_zero_start():
+    """The committed restart-mode network (corrections of the iterate after
+    100 plain iterations, trained on seeds 0..2047) on 32 held-out seeds:
+    the same stop test from both runs; the first 100 iterations count."""
+    from opymize_gb300.warmstart import UNet, evaluate_restart
+    net = UNet.load(WEIGHTS.replace("unet512.npz", "unet512_restart.npz"))
+    assert net.restart
+    seeds = range(2 * 10 ** 6, 2 * 10 ** 6 + 32)
+    for tol, ratio in ((1e-3, 0.8), (1e-4, 0.95)):
+        ev = evaluate_restart(net, seeds, 100, S=512, tol=tol)
+        assert ev["converged_cold"] == ev["converged_warm"] == 32
+        assert all(abs(r) < tol for r in ev["relgap_warm"])
+        it_c, it_w = np.array(ev["iters_cold"]), np.array(ev["iters_warm"])
+        assert it_w.mean() <= ratio * it_c.mean(), (tol, it_c.mean(), it_w.mean())
