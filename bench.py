@@ -420,6 +420,48 @@ def warm_start_case(a, n_eval=32):
     return res
 
 
+def ssn_case(a, newton_steps=3):
+    """Semismooth Newton (the reference's CPU-only method, here on the
+    device) on 256^2 gray ROF (lambda = 0.1, centered gradient as the
+    reference default) from 300 preconditioned PDHG iterations: time per
+    Newton step and CG iterations, beside the oracle's CPU restatement of one
+    step on the host (the reference's own code is numpy on one core)."""
+    import oracle
+    from oracle.ssn import SemismoothNewton as OracleSSN
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.functionals import SSD, L1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG, SemismoothNewton
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    t = torch()
+    dims = (256, 256)
+    N = dims[0] * dims[1]
+    f = piecewise_constant(dims, 1, sigma=0.1, seed=a.seed)
+    p = PDHG(SSD(f.reshape(N, 1)), L1Norms(N, (1, 2), 0.1), GradientOp(dims, 1))
+    p.solve(steps="precond", precision="double", term_pd_gap=1e-300, term_maxiter=300,
+            granularity=300)
+    start = np.concatenate([v.ravel() for v in p.state])
+    s = SemismoothNewton(SSD(f.reshape(N, 1)), L1Norms(N, (1, 2), 0.1), GradientOp(dims, 1))
+    np.random.seed(1)
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    info = s.solve(continue_at=start.copy(), granularity=newton_steps, term_relgap=1e-300,
+                   term_maxiter=newton_steps)
+    t.cuda.synchronize()
+    gpu_s = (time.perf_counter() - t0) / newton_steps
+    o = OracleSSN(f, 0.1, oracle.Gradient(dims, 1, "centered"), 2)
+    t0 = time.perf_counter()
+    o.solve(start, 1)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "semismooth Newton, ROF 256^2 gray, lambda 0.1, FP64, from 300 precond PDHG "
+                        "iterations", "newton_steps": newton_steps,
+            "gpu_s_per_step": round(gpu_s, 4), "cg_iters": s.cg_iters,
+            "relgap_start": p.info["relgap"], "relgap_after": info["relgap"],
+            "cpu_oracle_s_per_step": round(cpu_s, 3),
+            "note": "per step: normest once per solve, one CG solve (3 FP64 device inner products "
+                    "per CG iteration read by the host), Armijo search"}
+
+
 def e2e_solve(a, f):
     """The public-API call a user makes, host data in and out."""
     from opymize_gb300.functionals import SSD, HuberL1Norms
@@ -586,7 +628,8 @@ def run_gpu_arm(a, world, rank, local):
             out["other_workloads"] = {"volume_256x256x256": volume_case(a),
                                       "sublabel_512x512_L16": sublabel_case(a),
                                       "batched_512_instances": batch_case(a),
-                                      "warm_start_512x512": warm_start_case(a)}
+                                      "warm_start_512x512": warm_start_case(a),
+                                      "semismooth_newton_256x256": ssn_case(a)}
         if world == 1 and not a.no_cpu:
             cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs_iters)
             out["cpu_baseline"] = {

@@ -85,6 +85,8 @@ class DeviceArray(object):
                           src.ptr, out.ptr, stream_ptr())
             return out
         ary = np.ascontiguousarray(ary, dtype=want)
+        if not ary.flags.writeable:     # torch.from_numpy wants a writable buffer
+            ary = ary.copy()
         src = ary.view(np.uint8) if ary.dtype == np.bool_ else ary
         t = torch().from_numpy(src).to("cuda", non_blocking=False)
         return cls(t, np.uint8 if ary.dtype == np.bool_ else ary.dtype)
