@@ -417,15 +417,6 @@ __global__ void k_gelu_bwd(int64_t npix, int C, const float* __restrict__ da, in
   }
 }
 
-__global__ void k_colsum(const float* __restrict__ part, int nblk, int C, float* __restrict__ out,
-                         int accumulate) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
-  float s = 0.f;
-  for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * C + c];
-  out[c] = accumulate ? out[c] + s : s;
-}
-
 // ---- vectorised versions (8 bf16 or 4 fp32 channels per thread; channel
 // counts, strides and offsets multiples of 8, 16-byte aligned pointers)
 struct alignas(16) bf8 { bf16 v[8]; };

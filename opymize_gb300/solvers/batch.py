@@ -126,10 +126,6 @@ class BatchROF(object):
         _lib.call("opyx_rof_batch_init", desc[0].ctypes.data, desc[1].data_ptr(), stream_ptr())
         self.launches += 1
 
-    def _records(self):
-        rec = self.records.get().reshape(self.n, self.rec_bytes // 8)
-        return rec[:, 256 // 8:256 // 8 + len(_lib.ROF_INFO_FIELDS)]
-
     def autotune(self, iters=4):
         """Rows per work item: each candidate runs `iters` iterations from the
         zero start, timed with CUDA events; the fastest is kept and the state

@@ -92,7 +92,6 @@ class UNet(object):
             self.wt[name] = t.empty(9, cin, cout, device="cuda", dtype=t.bfloat16)
         self.steps = 0
         self._bufs = {}
-        self._ws = None
         self.loss_weights = t.tensor(LOSS_WEIGHTS, device="cuda", dtype=t.float32)
         self.refresh_weights()
 
