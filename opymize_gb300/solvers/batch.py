@@ -287,6 +287,38 @@ class BatchROF(object):
         return sum(H * W for H, W, _ in self.dims)
 
 
+def shard(sizes, rank, world):
+    """Indices of the instances rank `rank` of `world` solves: instances are
+    independent, so the batch splits across GPUs with no collective on the
+    data path.  Greedy by size (largest first onto the least loaded rank, ties
+    to the lower rank), deterministic on every rank."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank/world")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.empty(len(sizes), dtype=np.int64)
+    for i in sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k)):
+        r = int(np.argmin(load))
+        owner[i] = r
+        load[r] += sizes[i]
+    return [i for i in range(len(sizes)) if owner[i] == rank]
+
+
+def gather_stats(stats, group=None):
+    """The one collective of a sharded batch: every rank's stats (a
+    picklable object, e.g. {instance index: info}) gathered on all ranks;
+    without an initialised process group, [stats]."""
+    try:
+        import torch.distributed as dist
+    except ImportError:
+        return [stats]
+    if not dist.is_available() or not dist.is_initialized():
+        return [stats]
+    out = [None] * dist.get_world_size(group)
+    dist.all_gather_object(out, stats, group=group)
+    return out
+
+
 def _main(argv=None):
     """A seeded mixed-size batch (sides log-uniform in [64, 1024], aspect
     U[0.5, 2], lambda U[0.02, 0.3], sigma U[0.05, 0.2]) solved for a few
