@@ -453,6 +453,11 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
                             void* host_desc, size_t host_bytes, int* nitems);
 int opyx_rof_batch_init(const void* host_desc, const void* dev_desc, void* stream);
 int opyx_rof_batch_iterate(const void* host_desc, const void* dev_desc, int iters, void* stream);
+/* The iterations of one tile-width class (0: 128, 1: 256, 2: 512 pixels):
+ * classes hold disjoint instances, so a caller may run them on separate
+ * streams and join before the gap. */
+int opyx_rof_batch_iterate_class(const void* host_desc, const void* dev_desc, int cls, int iters,
+                                 void* stream);
 int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* partials,
                        void* stream);
 

@@ -175,6 +175,7 @@ SIGNATURES = {
                                       vp, sz, P(C.c_int)]),
     "opyx_rof_batch_init": (i32, [vp, vp, vp]),
     "opyx_rof_batch_iterate": (i32, [vp, vp, i32, vp]),
+    "opyx_rof_batch_iterate_class": (i32, [vp, vp, i32, i32, vp]),
     "opyx_rof_batch_gap": (i32, [vp, vp, vp, vp]),
     "opyx_conv3x3": (i32, [P(opyx_conv3x3_desc), vp]),
     "opyx_conv3x3_wgrad_workspace": (sz, [P(opyx_conv3x3_desc)]),

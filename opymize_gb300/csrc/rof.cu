@@ -912,6 +912,17 @@ static int batch_sweep_all(const BatchHeader& h, const BatchInst* insts, const B
   return st;
 }
 
+template <int C>
+static int batch_sweep_class(const BatchHeader& h, const BatchInst* insts, const BatchItem* items,
+                             int cls, int flip, cudaStream_t s) {
+  const int n = h.class_beg[cls + 1] - h.class_beg[cls];
+  if (!n) return OPYX_OK;
+  const BatchItem* it = items + h.class_beg[cls];
+  if (cls == 0) return batch_launch_sweep<C, 128>(insts, it, n, flip, s);
+  if (cls == 1) return batch_launch_sweep<C, 256>(insts, it, n, flip, s);
+  return batch_launch_sweep<C, 512>(insts, it, n, flip, s);
+}
+
 }  // namespace rof
 }  // namespace opyx
 
@@ -1027,6 +1038,30 @@ int opyx_rof_batch_iterate(const void* host_desc, const void* dev_desc, int iter
       case 2: st = batch_sweep_all<2>(h, insts, items, it & 1, s); break;
       case 3: st = batch_sweep_all<3>(h, insts, items, it & 1, s); break;
       case 4: st = batch_sweep_all<4>(h, insts, items, it & 1, s); break;
+      default: return OPYX_ERR_UNSUPPORTED;
+    }
+    if (st) return st;
+  }
+  return OPYX_OK;
+}
+
+int opyx_rof_batch_iterate_class(const void* host_desc, const void* dev_desc, int cls, int iters,
+                                 void* stream) {
+  if (!host_desc || !dev_desc || iters < 0 || (iters & 1) || cls < 0 || cls >= kBatchClasses)
+    return OPYX_ERR_ARG;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1 || h.nitems < 0) return OPYX_ERR_ARG;
+  if (h.nitems == 0 || iters == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)dev_desc + batch_inst_off());
+  const BatchItem* items = (const BatchItem*)((const char*)dev_desc + batch_item_off(h.ninst));
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int it = 0; it < iters; ++it) {
+    int st;
+    switch (h.nchannels) {
+      case 1: st = batch_sweep_class<1>(h, insts, items, cls, it & 1, s); break;
+      case 2: st = batch_sweep_class<2>(h, insts, items, cls, it & 1, s); break;
+      case 3: st = batch_sweep_class<3>(h, insts, items, cls, it & 1, s); break;
+      case 4: st = batch_sweep_class<4>(h, insts, items, cls, it & 1, s); break;
       default: return OPYX_ERR_UNSUPPORTED;
     }
     if (st) return st;

@@ -46,6 +46,7 @@ class BatchROF(object):
         g = 10 if granularity is None else int(granularity)
         self.gran = g + (g & 1)   # iterations run in pairs
         self.rows_per_item = rows_per_item
+        self.class_streams = True    # width classes on separate streams inside the graphs
         lib = _lib.load()
         self.problems = (_lib.opyx_rof_problem * self.n)()
         self.buffers = (_lib.opyx_rof_buffers * self.n)()
@@ -102,6 +103,7 @@ class BatchROF(object):
                   _lib.C.byref(nitems))
         cb = host[16:32].view(np.int32)              # the header's class_beg[0..3]
         self._classes = int(np.count_nonzero(np.diff(cb)))
+        self._class_ids = [c for c in range(3) if cb[c + 1] > cb[c]]
         t = torch()
         dev = t.from_numpy(host).to("cuda")
         part = DeviceArray.empty((max(1, nitems.value) * 5,), np.float64)
@@ -181,7 +183,27 @@ class BatchROF(object):
         graph = t.cuda.CUDAGraph()
         stream.wait_stream(t.cuda.current_stream())
         with t.cuda.graph(graph, stream=stream):
-            self._iterate(desc, nitems, n)
+            if len(self._class_ids) > 1 and self.class_streams:
+                # the classes' instances are disjoint: one chain of iterations
+                # per class on its own stream, joined before the gap
+                if not hasattr(self, "_side"):
+                    self._side = [t.cuda.Stream() for _ in range(3)]
+                fork = t.cuda.Event()
+                fork.record(stream)
+                joins = []
+                for c in self._class_ids:
+                    side = self._side[c]
+                    side.wait_event(fork)
+                    with t.cuda.stream(side):
+                        _lib.call("opyx_rof_batch_iterate_class", desc[0].ctypes.data,
+                                  desc[1].data_ptr(), c, n, stream_ptr())
+                        ev = t.cuda.Event()
+                        ev.record(side)
+                        joins.append(ev)
+                for ev in joins:
+                    stream.wait_event(ev)
+            else:
+                self._iterate(desc, nitems, n)
             self._gap(desc, nitems, part)
             self._pinned[slot].copy_(self.records.t, non_blocking=True)
         return graph
