@@ -97,17 +97,22 @@ class BatchROF(object):
         if st not in (_lib.OPYX_OK, _lib.OPYX_ERR_WORKSPACE):
             raise _lib.OpyxError("opyx_rof_batch_describe", st, _lib.status_string(st))
         nbytes = lib.opyx_rof_batch_desc_bytes(self.n, nitems.value)
-        host = np.zeros(nbytes, dtype=np.uint8)
+        t = torch()
+        # pinned host copy, uploaded without a synchronisation: chunks queued
+        # on the stream keep running on the previous descriptor (its device
+        # copy stays alive in their graphs' tuples) while this one is built
+        pinned = t.zeros(nbytes, dtype=t.uint8, pin_memory=True)
+        host = pinned.numpy()
         _lib.call("opyx_rof_batch_describe", self.problems, self.buffers, self.n,
                   self.records.ptr, act.ctypes.data, int(rows), host.ctypes.data, nbytes,
                   _lib.C.byref(nitems))
         cb = host[16:32].view(np.int32)              # the header's class_beg[0..3]
         self._classes = int(np.count_nonzero(np.diff(cb)))
         self._class_ids = [c for c in range(3) if cb[c + 1] > cb[c]]
-        t = torch()
-        dev = t.from_numpy(host).to("cuda")
+        dev = t.empty(nbytes, dtype=t.uint8, device="cuda")
+        dev.copy_(pinned, non_blocking=True)
         part = DeviceArray.empty((max(1, nitems.value) * 5,), np.float64)
-        return (host, dev), nitems.value, part
+        return (host, dev, pinned), nitems.value, part
 
     def _reset(self):
         for arr in self.arrays:
@@ -242,6 +247,8 @@ class BatchROF(object):
                                 pin_memory=True) for _ in range(self.DEPTH)]
         active = np.ones(self.n, np.uint8)
         desc, nitems, part = self._describe(active, self.rows_per_item)
+        described = active.copy()
+        self._pix = np.array([H * W for H, W, _ in self.dims], dtype=np.int64)
         self._init(desc)
         gran = self.gran
         graphs = None
@@ -281,10 +288,13 @@ class BatchROF(object):
             done = (last[:, i_done] != 0) & (active != 0)
             if done.any():
                 active[done] = 0
-                if active.any():
-                    # chunks already queued keep the old active set (finished
-                    # images are skipped on the device); new ones use the new one
+                # finished images are skipped on the device, so the descriptor
+                # is rebuilt only once a tenth of its pixels have finished;
+                # chunks already queued keep the previous one
+                gone = self._pix[(described != 0) & (active == 0)].sum()
+                if active.any() and gone >= 0.1 * self._pix[described != 0].sum():
                     desc, nitems, part = self._describe(active, self.rows_per_item)
+                    described = active.copy()
                     graphs = None
         t.cuda.synchronize()
         self.elapsed = time.perf_counter() - t0
