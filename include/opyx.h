@@ -432,9 +432,10 @@ int opyx_rof_pass(const opyx_rof_problem* p, const opyx_rof_buffers* b, int whic
  *   term_mode, `done`, `fault` as for single solves).
  * opyx_rof_batch_describe fills, ON THE HOST, a descriptor of
  *   opyx_rof_batch_desc_bytes(ninst, nitems) bytes: per instance its
- *   coefficients and pointers, and work items (rows_per_item rows x 128,
- *   256 or 512 pixels: the narrowest tile width that holds the instance's
- *   rows) for the instances with active[i] != 0 (all if active is NULL);
+ *   coefficients and pointers, and work items (rows_per_item rows x a
+ *   column tile: the instance's rows cut into equal tiles of at most 128,
+ *   256 or 512 pixels, in the width class that leaves the fewest lanes
+ *   idle) for the instances with active[i] != 0 (all if active is NULL);
  *   the caller copies it to device memory and passes both copies below (the
  *   host copy for the launch shapes, the device copy to the kernels).
  *   *nitems receives the work item count; with host_desc NULL and

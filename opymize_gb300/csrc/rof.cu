@@ -654,9 +654,9 @@ namespace rof {
 
 constexpr size_t kBatchRecord = 512;   // [0, 256) step state, [256, 512) info
 
-// Work items come in three tile-width classes (128, 256, 512 pixels), each
-// image in the narrowest class that holds its rows, so narrow images do not
-// leave most of a 512-pixel CTA idle; the sweep launches once per class.
+// Work items come in three tile-width classes (128, 256, 512 pixels; see
+// batch_tiles for the choice per image), so narrow images do not leave most
+// of a 512-pixel CTA idle; the sweep launches once per class.
 constexpr int kBatchClasses = 3;
 constexpr int kBatchTW[kBatchClasses] = {128, 256, 512};
 
