@@ -1072,13 +1072,14 @@ static int launch_wgrad(const CUtensorMap& xm, const CUtensorMap& dm, const WgAr
   return check_launch();
 }
 
+// The network kernels' sticky fault flag: a static device word (no
+// allocation), one per GPU that loads the library.
+__device__ unsigned g_net_fault;
+
 static unsigned* fault_word() {
-  static unsigned* f = nullptr;
-  if (!f) {
-    if (cudaMalloc(&f, sizeof(unsigned)) != cudaSuccess) return nullptr;
-    cudaMemset(f, 0, sizeof(unsigned));
-  }
-  return f;
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_net_fault) != cudaSuccess) return nullptr;
+  return (unsigned*)p;
 }
 
 // Pixel-tile ranges of the weight gradient: about two waves of CTAs.
