@@ -20,14 +20,45 @@ namespace epi {
 
 constexpr int kThreads = 128;
 constexpr int kEvalBlocks = 1024;
+constexpr int kCached = 8;
 
-template <typename T, int ND>
+// The constraints of one instance.  NS > 0 (nsub <= NS): read once into
+// registers by cache() -- the method scans them several times, and the rows
+// b[i, :] and I[i, :] of neighbouring threads lie a row apart, so every scan
+// from memory costs a warp one access per thread.  Slots past nsub are off.
+// NS = 0: read from memory at every scan.
+template <typename T, int ND, int NS>
 struct Inst {
   const T* v;          // (npoints, ND)
   const T* brow;       // b[i, :]
   const uint8_t* irow; // I[i, :]
   const int64_t* jrow; // J[j, :]
   int nsub;
+  static constexpr int NC = NS > 0 ? NS : 1;
+  T cv[NC][ND];
+  T cb[NC];
+  int cid[NC];
+  bool con[NC];
+
+  OPYX_D void cache() {
+    if constexpr (NS > 0) {
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        const bool used = k < nsub;
+        const int64_t l = used ? jrow[k] : 0;
+        cid[k] = (int)l;
+        con[k] = used && irow[l];
+#pragma unroll
+        for (int q = 0; q < ND; ++q) cv[k][q] = used ? v[l * ND + q] : T(0);
+        cb[k] = used ? brow[l] : T(0);
+      }
+    }
+  }
+  OPYX_D int count() const { return NS > 0 ? NS : nsub; }
+  OPYX_D int id(int k) const { return NS > 0 ? cid[k] : (int)jrow[k]; }
+  OPYX_D bool on(int k, int l) const { return NS > 0 ? con[k] : irow[l] != 0; }
+  OPYX_D const T* row(int k, int l) const { return NS > 0 ? cv[k] : v + (int64_t)l * ND; }
+  OPYX_D T b(int k, int l) const { return NS > 0 ? cb[k] : brow[l]; }
 };
 
 // a_l . y with a_l = (v[l], -1)
@@ -140,17 +171,26 @@ struct ActiveBasis {
   }
 };
 
-// Largest violation max_l (a_l . y - b_l) over the instance's constraints
-// and the constraint attaining it (-1 if none).
-template <typename T, int ND>
-OPYX_D T max_violation(const Inst<T, ND>& in, const T* y, int* arg) {
+// Largest violation max_l (a_l . y - b_l) over the instance's constraints,
+// the constraint attaining it (-1 if none) and its v_l (in wv, if given).
+template <typename T, int ND, int NS>
+OPYX_D T max_violation(const Inst<T, ND, NS>& in, const T* y, int* arg, T* wv = nullptr) {
   T worst = -INFINITY;
   *arg = -1;
-  for (int k = 0; k < in.nsub; ++k) {
-    const int64_t l = in.jrow[k];
-    if (!in.irow[l]) continue;
-    const T r = adot<T, ND>(in.v + l * ND, y) - in.brow[l];
-    if (r > worst) { worst = r; *arg = (int)l; }
+#pragma unroll(NS > 0 ? NS : 1)
+  for (int k = 0; k < in.count(); ++k) {
+    const int l = in.id(k);
+    if (!in.on(k, l)) continue;
+    const T* vl = in.row(k, l);
+    const T r = adot<T, ND>(vl, y) - in.b(k, l);
+    if (r > worst) {
+      worst = r;
+      *arg = l;
+      if (wv) {
+#pragma unroll
+        for (int q = 0; q < ND; ++q) wv[q] = vl[q];
+      }
+    }
   }
   return worst;
 }
@@ -166,8 +206,8 @@ OPYX_D T max_violation(const Inst<T, ND>& in, const T* y, int* arg) {
 // step" and step through it.  A claimed KKT point is accepted only if it is
 // feasible to the same precision; otherwise the instance is reported as
 // not converged.
-template <typename T, int ND>
-OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol) {
+template <typename T, int ND, int NS>
+OPYX_D bool project(const Inst<T, ND, NS>& in, const T* x, T* y, int maxiter, T tol) {
   constexpr int N1 = ND + 1, NA = ND + 1;
   constexpr T eps = sizeof(T) == 4 ? T(1.1920929e-7) : T(2.220446049250313e-16);
   const T tol_s = fmax(tol, T(64) * eps);           // step-fraction tolerance
@@ -178,7 +218,8 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
   const T tol_tight = T(8) * eps * xs;              // a constraint counts as tight
   // feasible start: raise the last coordinate by the largest violation
   int first;
-  const T viol = max_violation<T, ND>(in, x, &first);
+  T fv[ND];
+  const T viol = max_violation(in, x, &first, fv);
 #pragma unroll
   for (int k = 0; k < N1; ++k) y[k] = x[k];
   if (first < 0 || !(viol > T(0))) return true;  // feasible points are fixed
@@ -188,7 +229,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
   int m = 1;
   W[0] = first;
 #pragma unroll
-  for (int k = 0; k < ND; ++k) aw[0][k] = in.v[first * ND + k];
+  for (int k = 0; k < ND; ++k) aw[0][k] = fv[k];
   // the constraint dropped last: its negative multiplier says the next step
   // leaves it, so it does not take part in that step's ratio test (in FP32
   // a short step's direction is noisy enough to read as "into" it)
@@ -205,6 +246,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
 #pragma unroll
     for (int k = 0; k < N1; ++k) { pn += fabs(p[k]); dn += fabs(d[k]); }
     int blocking = -1;
+    T bv[ND];
     bool null_step = false;
     // a step at the rounding level of its own computation (|p| against
     // |x - y|) or below the tightness tolerance is noise: the multipliers
@@ -222,17 +264,18 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
       T smin = T(1);
       for (int pass = 0; pass < 2; ++pass) {
         T apb = T(0);
-        for (int k = 0; k < in.nsub; ++k) {
-          const int64_t l = in.jrow[k];
-          if (!in.irow[l]) continue;
+#pragma unroll(NS > 0 ? NS : 1)
+        for (int k = 0; k < in.count(); ++k) {
+          const int l = in.id(k);
+          if (!in.on(k, l)) continue;
           bool act = (int)l == dropped;
 #pragma unroll
           for (int a = 0; a < NA; ++a) act |= (a < m && W[a] == (int)l);
           if (act) continue;
-          const T* vl = in.v + l * ND;
+          const T* vl = in.row(k, l);
           const T ap = adot<T, ND>(vl, p);
           if (!(ap > tol_ap)) continue;
-          const T slack = in.brow[l] - adot<T, ND>(vl, y);
+          const T slack = in.b(k, l) - adot<T, ND>(vl, y);
           const T s = slack > tol_tight ? slack / ap : T(0);
           if (!(s > -tol_s)) continue;
           if (pass == 0) {
@@ -242,6 +285,8 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
             // errors of eps*|b|/slack, far above eps near a degenerate vertex)
             apb = ap;
             blocking = (int)l;
+#pragma unroll
+            for (int q = 0; q < ND; ++q) bv[q] = vl[q];
           }
         }
       }
@@ -255,7 +300,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
     if (blocking >= 0) {
       W[m] = blocking;
 #pragma unroll
-      for (int k = 0; k < ND; ++k) aw[m][k] = in.v[blocking * ND + k];
+      for (int k = 0; k < ND; ++k) aw[m][k] = bv[k];
       ++m;
       if (m < NA) continue;
     }
@@ -283,7 +328,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
       // a KKT point of the working set; it solves the full problem if it is
       // feasible (else a step crossed a constraint: reported, not hidden)
       int lv;
-      return !(max_violation<T, ND>(in, y, &lv) > tol_feas);
+      return !(max_violation(in, y, &lv) > tol_feas);
     }
     // drop the most negative multiplier
     dropped = W[amin];
@@ -295,7 +340,7 @@ OPYX_D bool project(const Inst<T, ND>& in, const T* x, T* y, int maxiter, T tol)
   return false;
 }
 
-template <typename T, int ND>
+template <typename T, int ND, int NS>
 __global__ void __launch_bounds__(kThreads)
 k_proj(opyx_epigraph e, const T* __restrict__ x, T* y, int maxiter, double tol,
        unsigned* nonconv) {
@@ -305,12 +350,13 @@ k_proj(opyx_epigraph e, const T* __restrict__ x, T* y, int maxiter, double tol,
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = t / e.nfuns, i = t - j * e.nfuns;
-    Inst<T, ND> in;
+    Inst<T, ND, NS> in;
     in.v = (const T*)e.v;
     in.brow = (const T*)e.b + i * e.npoints;
     in.irow = e.I + i * e.npoints;
     in.jrow = e.J + j * e.nsubpoints;
     in.nsub = e.nsubpoints;
+    in.cache();
     T xi[N1], yi[N1];
 #pragma unroll
     for (int k = 0; k < N1; ++k) xi[k] = x[t * N1 + k];
@@ -455,8 +501,13 @@ int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y
   if (!x || !y || maxiter < 1 || !(tol >= 0)) return OPYX_ERR_ARG;
   const unsigned g = grid_for(total, kThreads, 16);
   cudaStream_t s = (cudaStream_t)stream;
-#define OPYX_EPI_LAUNCH(TT, ND)                                                        \
-  k_proj<TT, ND><<<g, kThreads, 0, s>>>(*e, (const TT*)x, (TT*)y, maxiter, tol, nonconv)
+  // up to kCached constraints per instance are held in registers
+#define OPYX_EPI_LAUNCH(TT, ND)                                                          \
+  (e->nsubpoints <= kCached                                                              \
+       ? k_proj<TT, ND, kCached><<<g, kThreads, 0, s>>>(*e, (const TT*)x, (TT*)y, maxiter, \
+                                                        tol, nonconv)                     \
+       : k_proj<TT, ND, 0><<<g, kThreads, 0, s>>>(*e, (const TT*)x, (TT*)y, maxiter, tol,  \
+                                                  nonconv))
   if (dtype == OPYX_F32) {
     if (e->ndim == 1) OPYX_EPI_LAUNCH(float, 1);
     else if (e->ndim == 2) OPYX_EPI_LAUNCH(float, 2);

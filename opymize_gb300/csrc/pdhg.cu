@@ -13,6 +13,7 @@ namespace opyx {
 template <typename T>
 __global__ void k_take_step(int64_t n, T* __restrict__ zkp1, const T* __restrict__ zk, T dir,
                             StepT<T> step, const T* __restrict__ zg) {
+  step.load();
   GRID_STRIDE(i, n) zkp1[i] = zk[i] + dir * step.at(i) * zg[i];
 }
 
@@ -20,6 +21,7 @@ template <typename T>
 __global__ void k_dual_step(int64_t n, T* __restrict__ ykp1, const T* __restrict__ yk,
                             StepT<T> sigma, T theta, const T* __restrict__ ygkp1,
                             const T* __restrict__ ygk) {
+  sigma.load();
   GRID_STRIDE(i, n) {
     const T ybar = (T(1) + theta) * ygkp1[i] - theta * ygk[i];
     ykp1[i] = yk[i] + sigma.at(i) * ybar;
@@ -34,6 +36,7 @@ __global__ void __launch_bounds__(kRedThreads)
 k_residual_pair(int64_t n, StepT<T> a, const T* __restrict__ zk, const T* __restrict__ zkp1,
                 T b, const T* __restrict__ zgk, T c1, T c2, const T* __restrict__ zgkp1,
                 double* out, double* partials, unsigned* ticket) {
+  a.load();
   double s1 = 0.0, s2 = 0.0;
   GRID_STRIDE(i, n) {
     const T base = (zk[i] - zkp1[i]) / a.at(i) - b * zgk[i];

@@ -28,6 +28,7 @@ __global__ void k_shiftscale(int64_t n, const T* __restrict__ av, T a, const T* 
 template <typename T>
 __global__ void k_affine_prox(int64_t n, const T* __restrict__ av, T a, const T* __restrict__ cv,
                               T c, StepT<T> tau, const T* __restrict__ x, T* __restrict__ y) {
+  tau.load();
   GRID_STRIDE(i, n) {
     const T ai = av ? av[i] : a;
     const T ci = cv ? cv[i] : c;
@@ -39,6 +40,7 @@ template <typename T>
 __global__ void k_ssd_prox(int64_t N, int C, const T* __restrict__ f, const double* __restrict__ vol,
                            const uint8_t* __restrict__ mask, StepT<T> tau,
                            const T* __restrict__ x, T* __restrict__ y) {
+  tau.load();
   GRID_STRIDE(o, N * C) {
     const int k = (int)(o % C);
     const int64_t i = o / C;
@@ -83,6 +85,7 @@ __global__ void k_l1proj(int64_t N, int M1, int M2, T lbd, int spectral, T* __re
 
 template <typename T>
 __global__ void k_huber_conj(int64_t N, int m, T lbd, T alpha, StepT<T> sigma, T* __restrict__ x) {
+  sigma.load();
   GRID_STRIDE(i, N) {
     T* xi = x + i * (int64_t)m;
     for (int j = 0; j < m; ++j) xi[j] /= T(1) + sigma.at(i * (int64_t)m + j) * alpha / lbd;

@@ -16,6 +16,14 @@ struct StepT {
   T value;
   __host__ StepT(const opyx_step& s) : vec((const T*)s.vec), dev(s.dev), value((T)s.value) {}
   OPYX_D T at(int64_t i) const { return vec ? vec[i] : (dev ? (T)__ldg(dev) : value); }
+  // Read a device scalar once per thread: the conversion from FP64 is an
+  // FP64-pipe instruction, far too slow on GB300 to repeat per element.
+  OPYX_D void load() {
+    if (!vec && dev) {
+      value = (T)__ldg(dev);
+      dev = nullptr;
+    }
+  }
 };
 
 // SSD prox of one value with t = tau*vol: a*(x + t*f), a = 1/(1 + t)

@@ -54,7 +54,8 @@ class PDHG(object):
         (opymize/solvers/pdhg.py:229-315) on the GPU.
 
         Extra keywords: ``fused`` (None = automatic, False forces the generic
-        path) and ``graph`` (capture chunks of the fused path in CUDA graphs).
+        path) and ``graph`` (capture chunks of iterations in CUDA graphs, on
+        both paths).
         """
         if not use_gpu:
             raise NotImplementedError("opymize_gb300 has no CPU path: use_gpu must be True")
@@ -117,7 +118,7 @@ class PDHG(object):
         if use_fused:
             self._solve_fused(*args, graph=graph)
         else:
-            self._solve_generic(*args)
+            self._solve_generic(*args, graph=graph)
         return self.info
 
     @property
@@ -254,7 +255,7 @@ class PDHG(object):
 
     # ------------------------------------------------------------ generic
     def _solve_generic(self, dtype, steps, term_pd_gap, term_pd_res, pd_res_mode,
-                       term_maxiter, granularity, cbfun):
+                       term_maxiter, granularity, cbfun, graph=True):
         i, c = self.itervars, self.constvars
         v = {}
         v['xk'], v['yk'] = self._start(dtype)
@@ -286,35 +287,83 @@ class PDHG(object):
         ws = DeviceArray.zeros(((_lib.load().opyx_reduce_workspace_size() + 7) // 8,),
                                np.float64)
         theta = c['theta']
+
+        def iterate():
+            """Launch one iteration (pdhg.py:124-187) and swap the roles of
+            the k and k+1 buffers."""
+            s = stream_ptr()
+            _lib.call("opyx_take_step", v['xk'].dcode, v['xk'].size, v['xkp1'].ptr,
+                      v['xk'].ptr, -1, step_struct(tau, dtype), v['xgradk'].ptr, s)
+            gprox(v['xkp1'])
+            self.linop(v['xkp1'], v['ygradkp1'])
+            _lib.call("opyx_dual_step", v['yk'].dcode, v['yk'].size, v['ykp1'].ptr,
+                      v['yk'].ptr, step_struct(sigma, dtype), theta, v['ygradkp1'].ptr,
+                      v['ygradk'].ptr, s)
+            fconjprox(v['ykp1'])
+            self.linop.adjoint(v['ykp1'], v['xgradkp1'])
+            if st is not None:
+                _lib.call("opyx_residual_pair", v['xk'].dcode, v['xk'].size,
+                          step_struct(st.tau), v['xk'].ptr, v['xkp1'].ptr, 1.0,
+                          v['xgradk'].ptr, 1.0, 0.0, v['xgradkp1'].ptr, st.sums_ptr(0),
+                          ws.ptr, s)
+                _lib.call("opyx_residual_pair", v['yk'].dcode, v['yk'].size,
+                          step_struct(st.sigma), v['yk'].ptr, v['ykp1'].ptr, theta,
+                          v['ygradk'].ptr, theta, theta + 1.0, v['ygradkp1'].ptr,
+                          st.sums_ptr(2), ws.ptr, s)
+                _lib.call("opyx_adaptive_update", st.ptr, s)
+            swap(1)
+
+        def swap(n):
+            if n % 2:
+                for a_, b_ in (('xk', 'xkp1'), ('xgradk', 'xgradkp1'), ('yk', 'ykp1'),
+                               ('ygradk', 'ygradkp1')):
+                    v[a_], v[b_] = v[b_], v[a_]
+
+        # Between checks, iterations run as CUDA graphs of up to
+        # _GENERIC_CHUNK iterations, captured on first use for the buffer
+        # roles they start from (the parity of the iterations done): a replay
+        # is one launch where an iteration is a few dozen host calls.  The
+        # first iteration runs eagerly (it creates the operators' lazily
+        # uploaded tables); a capture that fails (an operator that reads
+        # device data on the host) leaves the solve eager.
+        graphs = {}
+        capture = bool(graph)
+        parity = 0
+
+        def run(n):
+            nonlocal parity, capture
+            while n > 0:
+                m = min(n, _GENERIC_CHUNK)
+                g = graphs.get((m, parity)) if capture else None
+                if g is None and capture:
+                    saved = dict(v)
+                    try:
+                        g = graphs[(m, parity)] = _GenericGraph(iterate, m)
+                    except Exception as err:          # noqa: BLE001
+                        logging.info("generic PDHG path stays eager: %s", err)
+                        capture, g = False, None
+                    v.update(saved)
+                if g is None:
+                    iterate()
+                    m = 1
+                else:
+                    g.launch()
+                    swap(m)
+                parity ^= m & 1
+                n -= m
+
         t0 = time.perf_counter()
         _iter = 0
         with GracefulInterruptHandler() as hdl:
             while _iter < term_maxiter:
-                _iter += 1
+                if _iter == 0:
+                    n = 1
+                else:
+                    nxt = min((_iter // granularity + 1) * granularity, term_maxiter)
+                    n = nxt - _iter
+                run(n)
+                _iter += n
                 check = (_iter % granularity == 0)
-                s = stream_ptr()
-                _lib.call("opyx_take_step", v['xk'].dcode, v['xk'].size, v['xkp1'].ptr,
-                          v['xk'].ptr, -1, step_struct(tau, dtype), v['xgradk'].ptr, s)
-                gprox(v['xkp1'])
-                self.linop(v['xkp1'], v['ygradkp1'])
-                _lib.call("opyx_dual_step", v['yk'].dcode, v['yk'].size, v['ykp1'].ptr,
-                          v['yk'].ptr, step_struct(sigma, dtype), theta, v['ygradkp1'].ptr,
-                          v['ygradk'].ptr, s)
-                fconjprox(v['ykp1'])
-                self.linop.adjoint(v['ykp1'], v['xgradkp1'])
-                if st is not None:
-                    _lib.call("opyx_residual_pair", v['xk'].dcode, v['xk'].size,
-                              step_struct(st.tau), v['xk'].ptr, v['xkp1'].ptr, 1.0,
-                              v['xgradk'].ptr, 1.0, 0.0, v['xgradkp1'].ptr, st.sums_ptr(0),
-                              ws.ptr, s)
-                    _lib.call("opyx_residual_pair", v['yk'].dcode, v['yk'].size,
-                              step_struct(st.sigma), v['yk'].ptr, v['ykp1'].ptr, theta,
-                              v['ygradk'].ptr, theta, theta + 1.0, v['ygradkp1'].ptr,
-                              st.sums_ptr(2), ws.ptr, s)
-                    _lib.call("opyx_adaptive_update", st.ptr, s)
-                for a_, b_ in (('xk', 'xkp1'), ('xgradk', 'xgradkp1'), ('yk', 'ykp1'),
-                               ('ygradk', 'ygradkp1')):
-                    v[a_], v[b_] = v[b_], v[a_]
                 if hdl.interrupted or check:
                     self.info['iter'] = _iter
                     if st is not None:
@@ -478,6 +527,29 @@ class _FusedLoop(object):
         else:
             t.cuda.current_stream().synchronize()
         return it, rec
+
+
+# iterations per CUDA graph of the generic path
+_GENERIC_CHUNK = 16
+
+
+class _GenericGraph(object):
+    """`n` generic iterations captured once into a CUDA graph on a private
+    capture stream (no host synchronisation may happen inside: the
+    iteration's launches only) and replayed on the current stream."""
+
+    def __init__(self, iterate, n):
+        t = torch()
+        self.stream = t.cuda.Stream()
+        self.graph = t.cuda.CUDAGraph()
+        self.stream.wait_stream(t.cuda.current_stream())
+        with t.cuda.graph(self.graph, stream=self.stream):
+            for _ in range(n):
+                iterate()
+        t.cuda.current_stream().wait_stream(self.stream)
+
+    def launch(self):
+        self.graph.replay()
 
 
 class _RofGraph(object):

@@ -165,6 +165,75 @@ def test_nonsquare_matrixmult_and_duplicate_labels(gpu):
     assert tol_ok(out.get(), ref.spmat.T.dot(y), np.float64)
 
 
+# Sizes with many CTAs (grid-stride loops), divisors that are not powers of
+# two, and tables too large for the per-CTA shared-memory copy (the per-use
+# FP64 path).
+EINSUM_MANY = [("mm", (5, 7), 50021), ("mm", (100, 100), 3001), ("mmr", (16, 1), 70001),
+               ("mmr", (1, 16), 70001), ("mmr", (3, 5), 40009), ("mmrb", (4, 3, 5), 9001),
+               ("tmmr", (3, 2, 4, 5), 7001), ("dmmr", (7,), 30011),
+               ("mmr", (3, 5), 400009), ("mmr", (50, 3), 20011), ("mmr", (100, 100), 3001)]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("case", range(len(EINSUM_MANY)))
+def test_einsum_many_ctas(gpu, case, dtype):
+    from opymize_gb300 import linear as L
+    kind, shape, N = EINSUM_MANY[case]
+    rng = np.random.default_rng(case)
+    A = rng.standard_normal(shape)
+    for trans in ((False,) if kind == "dmmr" else (False, True)):
+        if kind == "dmmr":
+            op, ref = L.DiagMatrixMultR(N, A), olin.DiagMatrixMultR(N, A)
+        else:
+            cls = {"mm": "MatrixMult", "mmr": "MatrixMultR", "mmrb": "MatrixMultRBatched",
+                   "tmmr": "TangledMatrixMultR"}[kind]
+            op, ref = getattr(L, cls)(N, A, trans), getattr(olin, cls)(N, A, trans)
+        x = rng.standard_normal(op.x.size)
+        y = rng.standard_normal(op.y.size)
+        Ax, ATy = np.zeros(op.y.size), np.zeros(op.x.size)
+        ref(x, Ax)
+        ref.adjoint(y, ATy)
+        got = gpu.DeviceArray.zeros((op.y.size,), dtype)
+        op(gpu.to_gpu(x, dtype), got)
+        assert tol_ok(got.get(), Ax, dtype), (kind, shape, trans)
+        got = gpu.DeviceArray.zeros((op.x.size,), dtype)
+        op.adjoint(gpu.to_gpu(y, dtype), got)
+        assert tol_ok(got.get(), ATy, dtype), (kind, shape, trans, "adjoint")
+
+
+# (K, N, J, M, L, P): the sublabel layout (P[j] = (j, j+1)); random labels with
+# duplicates; more labels than threads per CTA; more (j, l) pairs than the
+# per-CTA label lists take (the unlisted scatter); more pixel tiles than CTAs
+def _indexed_cases():
+    r = np.random.default_rng(11)
+    return [(16, 70001, 15, 2, 2, np.stack([np.arange(15), np.arange(1, 16)], 1)),
+            (9, 20011, 6, 3, 4, r.integers(0, 9, (6, 4))),
+            (300, 2001, 200, 1, 2, r.integers(0, 300, (200, 2))),
+            (5, 301, 2100, 1, 2, r.integers(0, 5, (2100, 2))),
+            (4, 400009, 3, 2, 2, r.integers(0, 4, (3, 2)))]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("case", range(5))
+def test_indexed_many_ctas(gpu, case, dtype):
+    from opymize_gb300 import linear as L
+    K, N, J, M, Ln, P = _indexed_cases()[case]
+    rng = np.random.default_rng(case)
+    B = rng.standard_normal((J, M, Ln))
+    op, ref = L.IndexedMult(K, N, B, P), olin.IndexedMult(K, N, B, P)
+    x = rng.standard_normal(op.x.size)
+    y = rng.standard_normal(op.y.size)
+    got = gpu.DeviceArray.zeros((op.y.size,), dtype)
+    op(gpu.to_gpu(x, dtype), got)
+    assert tol_ok(got.get(), ref.spmat.dot(x), dtype)
+    got = gpu.DeviceArray.zeros((op.x.size,), dtype)
+    op.adjoint(gpu.to_gpu(y, dtype), got)
+    assert tol_ok(got.get(), ref.spmat.T.dot(y), dtype)
+    # add=True accumulates onto the output
+    op.adjoint(gpu.to_gpu(y, dtype), got, add=True)
+    assert tol_ok(got.get(), 2 * ref.spmat.T.dot(y), dtype)
+
+
 L1_KEYS = sorted({k.split("/")[0] for k in OPS.files if k.startswith("l1proj_")})
 
 
