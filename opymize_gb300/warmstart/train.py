@@ -7,7 +7,7 @@ gap) to a tight relative gap; the targets are (x* - f, y* / lambda).
 
 Evaluation: held-out seeds solved to relative gap 1e-4 from zero and from
 the network's proposal, by the same solver with the same stop test, so the
-plain method stays the judge of the warm start: a proposal only changes
+plain method stays the arbiter of the warm start: a proposal only changes
 where the iteration starts, never the accepted gap.
 """
 

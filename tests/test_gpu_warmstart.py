@@ -2,7 +2,7 @@
 gradient (tcgen05 convolutions, hand-written backward) against torch CPU
 autograd in FP64 on the same weights; training lowers the loss; the trained
 network's proposals let the fused PDHG reach the same relative gap in fewer
-iterations than the zero start, with the plain solver's stop test as judge."""
+iterations than the zero start, with the plain solver's stop test deciding."""
 
 import os
 
