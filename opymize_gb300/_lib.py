@@ -15,8 +15,12 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libopyx.so")
 
 OPYX_OK = 0
+OPYX_ERR_ARG = 1
 OPYX_ERR_LAUNCH = 2
+OPYX_ERR_UNSUPPORTED = 3
 OPYX_ERR_WORKSPACE = 4
+OPYX_ERR_NOT_CONVERGED = 5
+OPYX_ERR_SCRATCH_LIMIT = 6
 OPYX_F32, OPYX_F64 = 0, 1
 SCHEME = {"forward": 0, "centered": 1}
 BC = {"neumann": 0, "curvature": 1, "second-order": 2}
