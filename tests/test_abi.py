@@ -4,6 +4,7 @@ opymize_gb300/_lib.py binds them all, and the ctypes structures have the
 sizes and field offsets that a C compiler gives the header's structs.  No
 compute call is made (no GPU here)."""
 
+import ctypes as C
 import os
 import re
 import shutil
@@ -96,3 +97,76 @@ def test_no_cpu_fallback_without_gpu():
     s = PDHG(SSD(np.zeros((20, 1))), L1Norms(20, (1, 2), 0.1), op)
     with pytest.raises(NotImplementedError):
         s.solve(use_gpu=False)
+
+
+# Fake device addresses: aligned, never dereferenced, because each call below
+# fails its argument checks (or has no work) before it touches the device.
+_P = 1 << 40
+
+
+def _grid(ndim=2, dims=(4, 5), h=1.0, C=1):
+    g = _lib.opyx_grid()
+    g.ndim, g.nchannels = ndim, C
+    for t in range(min(ndim, len(dims))):
+        g.dims[t], g.h[t] = dims[t], h
+    return g
+
+
+def _epigraph(ndim=1, nsub=2, nfuns=3, nregions=2, npoints=3):
+    e = _lib.opyx_epigraph()
+    e.ndim, e.nsubpoints, e.nfuns, e.nregions, e.npoints = ndim, nsub, nfuns, nregions, npoints
+    e.I, e.J, e.v, e.b = _P, _P + 4096, _P + 8192, _P + 12288
+    return e
+
+
+def _conv(**kw):
+    d = _lib.opyx_conv3x3_desc()
+    d.batch, d.height, d.width = 1, 8, 8
+    d.in_channels = d.in_stride = 32
+    d.out_channels = d.out_stride = 32
+    d.x, d.w, d.y = _P, _P + 65536, _P + 131072
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+ARG, UNSUP, WS, OK = (_lib.OPYX_ERR_ARG, _lib.OPYX_ERR_UNSUPPORTED, _lib.OPYX_ERR_WORKSPACE,
+                      _lib.OPYX_OK)
+
+ERROR_CASES = [
+    ("opyx_fill", (0, None, 10, 0.0, None), ARG),
+    ("opyx_fill", (0, None, 0, 0.0, None), OK),                         # nothing to do
+    ("opyx_axpby", (0, -1, 1.0, _P, 0.0, _P, None), ARG),
+    ("opyx_matrixmult", (0, -1, 2, 2, _P, 0, _P, _P, 0, None), ARG),
+    ("opyx_matrixmult", (0, 10, 0, 2, _P, 0, _P, _P, 0, None), OK),     # J = 0: no output
+    ("opyx_matrixmultr", (0, 10, 2, 2, None, 0, _P, _P, 0, None), ARG),
+    ("opyx_matrixmultr", (7, 10, 2, 2, _P, 0, _P, _P, 0, None), ARG),    # unknown dtype
+    ("opyx_indexedmult", (0, 2, 10, 1, 1, 0, _P, _P, _P, _P, 0, None), ARG),      # K < 1
+    ("opyx_indexedmult_adj", (0, 2, 10, 1, 1, 0, _P, _P, _P, _P, 0, None), ARG),
+    ("opyx_indexedmult_adj", (0, 2, 10, 1, 1, 3, _P, None, _P, _P, 0, None), ARG),  # no P
+    ("opyx_l1normsproj", (0, 10, 1, 2, 0.1, 99, _P, None), ARG),       # unknown norm
+    ("opyx_l1normsproj", (0, 10, 3, 3, 0.1, 1, _P, None), UNSUP),      # spectral, 3 x 3
+    ("opyx_l1normsproj_jac", (0, 10, 2, 0.0, _P, _P, _P, None), ARG),  # lbd <= 0
+    ("opyx_dot", (0, 10, _P, _P, _P, _P + 4, None), WS),               # misaligned workspace
+    ("opyx_dot", (0, 10, _P, _P, None, _P, None), ARG),
+    ("opyx_gradient", (None, 0, None, 0, _P, _P, 0, None), ARG),
+    ("opyx_gradient", (_grid(h=0.0), 0, None, 0, _P, _P, 0, None), ARG),
+    ("opyx_gradient", (_grid(), 9, None, 0, _P, _P, 0, None), ARG),    # unknown scheme
+    ("opyx_epigraph_proj", (_epigraph(ndim=4), 0, _P, _P, 10, 1e-9, None, None), UNSUP),
+    ("opyx_epigraph_proj", (_epigraph(), 0, _P, _P, 0, 1e-9, None, None), ARG),  # maxiter 0
+    ("opyx_epigraph_proj", (_epigraph(nregions=0), 0, _P, _P, 10, 1e-9, None, None), OK),
+    ("opyx_conv3x3", (None, None), ARG),
+    ("opyx_conv3x3", (_conv(in_channels=24, in_stride=24), None), ARG),  # channels per chunk
+    ("opyx_conv3x3", (_conv(out_channels=48, out_stride=48), None), UNSUP),
+    ("opyx_conv3x3", (_conv(x=_P + 8), None), ARG),                    # 16-byte alignment
+]
+
+
+@pytest.mark.parametrize("case", range(len(ERROR_CASES)))
+def test_argument_checks_precede_device_work(lib, case):
+    """The entry points' error behaviour: invalid arguments return their
+    status without a launch (the reference's PyCUDA kernels return none;
+    this boundary reports one per call, see opyx_status_string)."""
+    name, args, want = ERROR_CASES[case]
+    args = tuple(C.byref(a) if isinstance(a, C.Structure) else a for a in args)
+    assert getattr(lib, name)(*args) == want, (name, _lib.status_string(getattr(lib, name)(*args)))
