@@ -86,6 +86,15 @@ class BatchROF(object):
         self.launches = 0
         self.info = []
 
+    @classmethod
+    def check_interval(cls, t_gap, t_iter):
+        """Iterations between stop tests for a test costing t_gap and an
+        iteration costing t_iter (any one time unit): g = sqrt(2 n t_gap /
+        t_iter) for n = GRAN_PRIOR_ITERS, rounded, made even (iterations run
+        in pairs) and clipped to GRAN_RANGE."""
+        g = int(round(np.sqrt(2.0 * cls.GRAN_PRIOR_ITERS * t_gap / max(t_iter, 1e-9))))
+        return int(np.clip(g + (g & 1), *cls.GRAN_RANGE))
+
     # ------------------------------------------------------------ plumbing
     def _describe(self, active, rows):
         lib = _lib.load()
@@ -169,8 +178,7 @@ class BatchROF(object):
             t.cuda.synchronize()
             t_gap = e0.elapsed_time(e1) / 3
             t_it = best[0] / iters
-            g = int(round(np.sqrt(2.0 * self.GRAN_PRIOR_ITERS * t_gap / max(t_it, 1e-9))))
-            g = int(np.clip(g + (g & 1), *self.GRAN_RANGE))
+            g = self.check_interval(t_gap, t_it)
             self.gran = g
             self.tuning.update(ms_per_gap=t_gap, granularity=g)
         self._reset()

@@ -73,3 +73,17 @@ def test_fused_path_selection():
     lap = LaplacianOp((4, 5), 1)
     assert not PDHG(SSD(f), SSD(np.zeros((20, 1))), lap)._fusable()
     assert not PDHG(SSD(f), QuadEpiInd(20, 1), GradientOp((4, 5), 1, "forward"))._fusable()
+
+
+def test_batch_check_interval():
+    """The batch autotuner's interval between stop tests: sqrt(2 n t_gap /
+    t_iter) for n = 1000 assumed iterations, even, within [10, 100]."""
+    from opymize_gb300.solvers.batch import BatchROF
+    assert BatchROF.check_interval(1.0, 1.0) == 46           # sqrt(2000) = 44.7 -> 45 -> 46
+    assert BatchROF.check_interval(0.5, 1.0) == 32           # sqrt(1000) = 31.6 -> 32
+    assert BatchROF.check_interval(1e-6, 1.0) == 10
+    assert BatchROF.check_interval(50.0, 1.0) == 100
+    assert BatchROF.check_interval(1.0, 0.0) == 100          # no division by zero
+    for t_gap in np.geomspace(1e-3, 10.0, 40):
+        g = BatchROF.check_interval(t_gap, 0.37)
+        assert g % 2 == 0 and 10 <= g <= 100
