@@ -192,6 +192,24 @@ int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y
 int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void* x,
                        double* out, void* ws, void* stream);
 
+/* ------------------------------------------- piecewise convexification (host) */
+/* The lower convex hull of every function's graph over every region, the
+ * input data of EpigraphInd / EpigraphSupp (I = base, If = faces):
+ * piecewise_convexify (opymize/quickhull/__init__.pyx:8-140, hull code
+ * convexhull.cpp:118-216).  HOST code: every pointer is host memory and no
+ * device work is done.  points (npoints, ndim) doubles, vals (nfuns, npoints)
+ * doubles, regions (nregions, nsub) indices into the points, the first ndim+1
+ * of each region its simplex's vertices.  Outputs: base (nfuns, npoints) 0/1;
+ * faces (nfuns, nregions, max_faces, ndim+1) positions in the region's row of
+ * `regions` (-1 past the count), nfaces (nfuns, nregions).  ndim 1 and 2
+ * (3 is OPYX_ERR_UNSUPPORTED: the reference needs Qhull's 4-D hull for it);
+ * max_faces >= opyx_convexify_max_faces(ndim, nsub), else
+ * OPYX_ERR_WORKSPACE; nthreads <= 0 uses every host thread. */
+int opyx_convexify_max_faces(int ndim, int nsub);
+int opyx_convexify(int ndim, int64_t npoints, const double* points, int64_t nfuns,
+                   const double* vals, int64_t nregions, int nsub, const int64_t* regions,
+                   uint8_t* base, int32_t* faces, int32_t* nfaces, int max_faces, int nthreads);
+
 /* ------------------------------------------------------------- step sizes */
 /* A step size is a per-element device vector (`vec`, of the iterate dtype,
  * preconditioned steps), else a device double written by the solver

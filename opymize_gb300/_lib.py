@@ -165,6 +165,8 @@ SIGNATURES = {
     "opyx_fct_eval": (i32, [P(opyx_fct), i32, vp, vp, vp, vp]),
     "opyx_epigraph_proj": (i32, [P(opyx_epigraph), i32, vp, vp, i32, f64, vp, vp]),
     "opyx_epigraph_eval": (i32, [P(opyx_epigraph), i32, i32, vp, vp, vp, vp]),
+    "opyx_convexify_max_faces": (i32, [i32, i32]),
+    "opyx_convexify": (i32, [i32, i64, vp, i64, vp, i64, i32, vp, vp, vp, vp, i32, i32]),
     "opyx_rof_workspace_size": (sz, []),
     "opyx_rof_info_offset": (sz, []),
     "opyx_rof_init": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), vp]),

@@ -92,9 +92,11 @@ def lower_hull_faces(d, i, j):
 
 
 def faces(d):
-    """If[i][j] for every pixel and interval (host loop: small problems)."""
-    N, L = d["b"].shape[0], d["L"]
-    return [[lower_hull_faces(d, i, j) for j in range(L - 1)] for i in range(N)]
+    """If[i][j] for every pixel and interval: the lower hulls of
+    `piecewise_convexify` (libopyx host code, every host thread), which are
+    those of `lower_hull_faces`."""
+    from opymize_gb300.tools.convexify import piecewise_convexify
+    return piecewise_convexify(d["v"], d["b"], d["J"])[1]
 
 
 def sublabel_problem(f_img, L=16, lbd=0.1, samples=8, trunc=0.04, with_faces=False):
