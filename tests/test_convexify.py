@@ -185,3 +185,24 @@ def test_sublabel_faces_match_lifting():
             for j in range(L - 1):
                 ref = lifting.lower_hull_faces(d, i, j)
                 assert faces[i][j].dtype == ref.dtype and np.array_equal(faces[i][j], ref), (i, j)
+
+
+def test_degenerate_inputs():
+    """Collinear corners, repeated points and non-finite values neither fail
+    nor leave the documented output ranges."""
+    pts = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0], [0.5, 0.0], [1.5, 0.0]])   # on a line
+    vals = np.array([[0.0, 1.0, 0.0, -1.0, 2.0], [np.nan, 0.0, 1.0, 0.0, np.inf]])
+    base, faces = piecewise_convexify(pts, vals, np.array([[0, 1, 2, 3, 4]]))
+    assert base[:, :3].all()
+    for fi in faces:
+        assert all(f.shape[1] == 3 and f.min() >= 0 and f.max() < 5 for f in fi)
+    pts = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [0.2, 0.2], [0.2, 0.2], [0.2, 0.2]])
+    vals = np.array([[0.0, 0.0, 0.0, -1.0, -1.0, -1.0], [0.0, 0.0, 0.0, -1.0, -2.0, -1.0]])
+    base, faces = piecewise_convexify(pts, vals, np.array([[0, 1, 2, 3, 4, 5]]))
+    assert base[:, :3].all() and base[1, 4]
+    for fi in faces:
+        f = fi[0]
+        assert f.shape[1] == 3 and f.min() >= 0 and f.max() < 6
+    x = np.array([[0.0], [1.0], [0.5], [0.5]])                                      # repeated abscissa
+    base, faces = piecewise_convexify(x, np.array([[0.0, 0.0, -1.0, -2.0]]), np.array([[0, 1, 2, 3]]))
+    assert base[0, 0] and base[0, 1] and base[0, 3]
