@@ -10,6 +10,7 @@ import pytest
 
 from oracle import convexify as ocvx
 from opymize_gb300.tools.convexify import piecewise_convexify, convexify_arrays
+from opymize_gb300.quickhull import piecewise_convexify as piecewise_convexify_ref_path
 
 
 def barygrid(ndim, nse):
@@ -206,3 +207,7 @@ def test_degenerate_inputs():
     x = np.array([[0.0], [1.0], [0.5], [0.5]])                                      # repeated abscissa
     base, faces = piecewise_convexify(x, np.array([[0.0, 0.0, -1.0, -2.0]]), np.array([[0, 1, 2, 3]]))
     assert base[0, 0] and base[0, 1] and base[0, 3]
+
+
+def test_reference_module_path():
+    assert piecewise_convexify_ref_path is piecewise_convexify
