@@ -45,6 +45,7 @@ class PDHG(object):
         self.use_gpu = True
         self.info = {}
         self.path = None
+        self.graph_replays = 0      # generic path: CUDA graph launches of the last solve
 
     # ------------------------------------------------------------------ API
     def solve(self, continue_at=None, precision="double", steps="const", step_bound=None,
@@ -319,13 +320,16 @@ class PDHG(object):
                                ('ygradk', 'ygradkp1')):
                     v[a_], v[b_] = v[b_], v[a_]
 
-        # Between checks, iterations run as CUDA graphs of up to
-        # _GENERIC_CHUNK iterations, captured on first use for the buffer
-        # roles they start from (the parity of the iterations done): a replay
-        # is one launch where an iteration is a few dozen host calls.  The
-        # first iteration runs eagerly (it creates the operators' lazily
-        # uploaded tables); a capture that fails (an operator that reads
-        # device data on the host) leaves the solve eager.
+        # Between checks, iterations run as CUDA graphs of _GENERIC_CHUNK
+        # iterations (one of a single iteration for odd remainders), captured
+        # on first use for the buffer roles they start from (the parity of
+        # the iterations done) and replayed back to back: a replay is one
+        # launch where an iteration is a few dozen host calls.  Capturing runs
+        # the host code of every iteration it records, so short graphs keep a
+        # solve's capture cost at a few iterations.  The first iteration runs
+        # eagerly (it creates the operators' lazily uploaded tables); a capture
+        # that fails (an operator that reads device data on the host) leaves
+        # the solve eager.
         graphs = {}
         capture = bool(graph)
         parity = 0
@@ -349,19 +353,22 @@ class PDHG(object):
                 else:
                     g.launch()
                     swap(m)
+                    self.graph_replays += 1
                 parity ^= m & 1
                 n -= m
 
+        self.graph_replays = 0
         t0 = time.perf_counter()
         _iter = 0
         with GracefulInterruptHandler() as hdl:
             while _iter < term_maxiter:
                 if _iter == 0:
-                    n = 1
+                    iterate()               # eager: the operators' first calls upload their tables
+                    parity, n = 1, 1
                 else:
                     nxt = min((_iter // granularity + 1) * granularity, term_maxiter)
                     n = nxt - _iter
-                run(n)
+                    run(n)
                 _iter += n
                 check = (_iter % granularity == 0)
                 if hdl.interrupted or check:
@@ -529,8 +536,9 @@ class _FusedLoop(object):
         return it, rec
 
 
-# iterations per CUDA graph of the generic path
-_GENERIC_CHUNK = 16
+# iterations per CUDA graph of the generic path (even: a replay keeps the
+# buffer roles)
+_GENERIC_CHUNK = 2
 
 
 class _GenericGraph(object):

@@ -243,9 +243,10 @@ def test_graph_and_eager_agree():
 @pytest.mark.parametrize("case", ["g2d_const_fwd", "g2d_precond_fwd", "c2d_huber_adaptive"])
 @pytest.mark.parametrize("precision", ["double", "float"])
 def test_generic_graph_and_eager_agree(case, precision):
-    """The generic path's CUDA graphs (chunks of up to 16 iterations, both
-    buffer parities, a remainder chunk before each check) replay the eager
-    iterations exactly: same state at every check, same final state."""
+    """The generic path's CUDA graphs (two-iteration graphs replayed back to
+    back, one-iteration graphs for odd remainders, both buffer parities)
+    replay the eager iterations exactly: same state at every check, same
+    final state."""
     from opymize_gb300.solvers import PDHG
     d = np.load(os.path.join(GOLDEN, case + ".npz"))
     out = []
@@ -258,6 +259,9 @@ def test_generic_graph_and_eager_agree(case, precision):
                 granularity=23, fused=False, graph=graph,
                 cbfun=lambda st, info: rec.append((st[0].copy(), st[1].copy(), info["iter"])))
         assert s.path == "generic" and s.info["iter"] == 61
+        # graphs in use: (22 + 23 + 15) iterations after the eager first one,
+        # in pairs and a single one per odd remainder
+        assert s.graph_replays == (11 + 12 + 8 if graph else 0)
         out.append((rec, s.state[0].copy(), s.state[1].copy()))
     (r1, x1, y1), (r2, x2, y2) = out
     assert [r[2] for r in r1] == [r[2] for r in r2] == [23, 46]
