@@ -123,3 +123,31 @@ def test_large_lifted_problem(dtype):
             yo, ok = E.project_polyhedron(x[j, i], A, bb, 2)
             assert ok
             assert np.abs(y[j, i] - yo).max() <= (1e-10 if dtype == np.float64 else 1e-5)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("samples", [5, 8, 12])
+def test_sublabel_instances_both_constraint_paths(dtype, samples):
+    """Sublabel-model instances with 5, 8 and 12 points per interval: up to 8
+    constraints per instance are held in registers, more are read from
+    memory at every scan; both against the oracle's projection."""
+    from opymize_gb300 import DeviceArray
+    from opymize_gb300.operators import EpigraphProj
+    from opymize_gb300.tools import lifting
+    rng = np.random.default_rng(samples)
+    nfuns = 3000
+    d = lifting.sublabel_data(rng.uniform(0, 1, nfuns), L=6, samples=samples, trunc=0.04)
+    I, J, v, b = d["I"], d["J"], d["v"], d["b"]
+    x = rng.normal(0, 0.5, (J.shape[0], nfuns, 2))
+    op = EpigraphProj(I, J, v, b)
+    yd = DeviceArray.zeros((x.size,), dtype)
+    op(DeviceArray.to_gpu(x.ravel(), dtype), yd)
+    y = yd.get().reshape(x.shape)
+    assert op.nonconverged == 0
+    for i in rng.choice(nfuns, 150, replace=False):
+        for j in range(J.shape[0]):
+            A, bb, _ = E.instance_constraints(I, J, v, b, j, i)
+            yo, ok = E.project_polyhedron(x[j, i], A, bb)
+            assert ok
+            assert np.abs(y[j, i] - yo).max() <= (1e-10 if dtype == np.float64
+                                                   else 2e-5 * max(1.0, np.abs(x).max()))
