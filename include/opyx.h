@@ -201,8 +201,7 @@ int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void*
  * doubles, regions (nregions, nsub) indices into the points, the first ndim+1
  * of each region its simplex's vertices.  Outputs: base (nfuns, npoints) 0/1;
  * faces (nfuns, nregions, max_faces, ndim+1) positions in the region's row of
- * `regions` (-1 past the count), nfaces (nfuns, nregions).  ndim 1 and 2
- * (3 is OPYX_ERR_UNSUPPORTED: the reference needs Qhull's 4-D hull for it);
+ * `regions` (-1 past the count), nfaces (nfuns, nregions).  ndim 1, 2 or 3;
  * max_faces >= opyx_convexify_max_faces(ndim, nsub), else
  * OPYX_ERR_WORKSPACE; nthreads <= 0 uses every host thread. */
 int opyx_convexify_max_faces(int ndim, int nsub);

@@ -4,8 +4,8 @@ faces that `EpigraphInd` / `EpigraphSupp` take as ``I`` and ``If``
 
 The hulls are computed by libopyx's host code (`opyx_convexify`, every host
 thread): this is set-up work on the host in the reference too (Cython over
-C++), not part of the GPU iteration.  1-D and 2-D points are supported; the
-reference's 3-D path needs Qhull's 4-D hull and is not provided.
+C++), not part of the GPU iteration.  Points of 1, 2 or 3 dimensions, as in
+the reference.
 """
 
 import ctypes as C
@@ -29,13 +29,10 @@ def convexify_arrays(points, vals, regions, nthreads=0):
     nregions, nsub = regions.shape
     if vals.shape[1] != npoints:
         raise ValueError("vals must be (nfuns, npoints)")
-    if ndim == 3:
-        raise NotImplementedError("3-D convexification needs a 4-D convex hull "
-                                  "(Qhull in the reference); 1-D and 2-D are supported")
     lib = _lib.load()
     mf = lib.opyx_convexify_max_faces(ndim, nsub)
     if mf < 1:
-        raise ValueError("regions need at least ndim+1 points, ndim 1 or 2")
+        raise ValueError("regions need at least ndim+1 points, ndim 1, 2 or 3")
     base = np.empty((nfuns, npoints), dtype=np.uint8)
     faces = np.empty((nfuns, nregions, mf, ndim + 1), dtype=np.int32)
     nfaces = np.empty((nfuns, nregions), dtype=np.int32)

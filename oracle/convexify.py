@@ -8,19 +8,20 @@ Restates opymize/quickhull/__init__.pyx:8-140 with its hull code
   convexhull.cpp:192-216): per region the points sorted by abscissa, per
   function a gift wrap from the leftmost point that steps to the point of
   smallest slope (slopes rounded to a 1e-9 grid, ties to the farthest point).
-* 2-D (`piecewise_convexify_nd`, __init__.pyx:85-140; getConvexHullND,
-  convexhull.cpp:118-183): the convex hull of the region's graph points plus
-  an apex above their centroid -- computed here with scipy's Qhull (option
-  Qt, triangulated facets) where the reference calls QuickHull -- and the
+* 2-D and 3-D (`piecewise_convexify_nd`, __init__.pyx:85-140;
+  getConvexHullND, convexhull.cpp:118-183): the convex hull of the region's
+  graph points plus an apex above their centroid -- computed here with
+  scipy's Qhull (option Qt, triangulated facets), which the reference calls
+  for 3-D points and where it calls QuickHull for 2-D -- and the
   reference's face filter: a face counts when its sorted vertices are not the
-  corner triangle, every vertex is a corner or lies more than 1e-9 below the
-  corners' plane (tested lazily, in face order, as is_base_face does) and its
-  unit lower normal points down by more than 1e-9.
+  corner simplex, every vertex is a corner or lies more than 1e-9 below the
+  corners' hyperplane (tested lazily, in face order, as is_base_face does)
+  and its unit lower normal points down by more than 1e-9.
 
 Pinned to the known answers of the reference's tests/convexhull.py (restated
-in tests/test_convexify.py).  The 2-D face sets depend on the hull library's
-triangulation of coplanar facets; on points in general position they are
-unique.
+in tests/test_convexify.py).  The 2-D and 3-D face sets depend on the hull
+library's triangulation of coplanar facets; on points in general position
+they are unique.
 """
 
 import numpy as np
@@ -60,8 +61,13 @@ def convexify_1d(points, vals, regions):
 
 
 def _lower_normal(v):
-    n = np.cross(v[1] - v[0], v[2] - v[0])
-    if n[2] > 0:
+    """Downward normal of the hyperplane through the rows of v (DIM x DIM),
+    by cofactors (hodge_3d / hodge_4d, convexhull.cpp:30-60), normalised
+    unless its squared length is below TOL."""
+    dim = v.shape[1]
+    d = v[1:] - v[0]
+    n = np.array([(-1) ** k * np.linalg.det(np.delete(d, k, axis=1)) for k in range(dim)])
+    if n[-1] > 0:
         n = -n
     nn = np.dot(n, n)
     if nn >= TOL:
@@ -69,31 +75,34 @@ def _lower_normal(v):
     return n
 
 
-def convexify_2d(points, vals, regions):
+def convexify_nd(points, vals, regions):
+    """2-D and 3-D points: __init__.pyx:85-140 with convexhull.cpp:118-183."""
     from scipy.spatial import ConvexHull
     nfuns, npoints = vals.shape
+    ndim = points.shape[1]
+    dim = ndim + 1
     nsub = regions.shape[1]
     base = np.zeros((nfuns, npoints), dtype=bool)
     faces = [[] for _ in range(nfuns)]
     for reg in regions:
-        g = np.zeros((nsub + 1, 3))
-        g[:nsub, :2] = points[reg]
-        g[nsub, :2] = g[:nsub, :2].sum(axis=0) / nsub
+        g = np.zeros((nsub + 1, dim))
+        g[:nsub, :ndim] = points[reg]
+        g[nsub, :ndim] = g[:nsub, :ndim].sum(axis=0) / nsub
         for i in range(nfuns):
-            g[:nsub, 2] = vals[i, reg]
-            if np.all(g[:nsub, 2] == g[0, 2]):
-                faces[i].append(np.arange(3)[None])
-                base[i, reg[:3]] = True
+            g[:nsub, ndim] = vals[i, reg]
+            if np.all(g[:nsub, ndim] == g[0, ndim]):
+                faces[i].append(np.arange(dim)[None])
+                base[i, reg[:dim]] = True
                 continue
-            g[nsub, 2] = g[:nsub, 2].max() + 0.1
+            g[nsub, ndim] = g[:nsub, ndim].max() + 0.1
             simplices = ConvexHull(g, qhull_options="Qt").simplices
-            n_c = _lower_normal(g[:3])
+            n_c = _lower_normal(g[:dim])
             c = np.dot(g[0], n_c) + TOL
-            b = np.array([1] * 3 + [2] * (nsub - 2))      # 2 = not tested yet
+            b = np.array([1] * dim + [2] * (nsub + 1 - dim))      # 2 = not tested yet
             keep = []
             for f in simplices:
                 f = np.sort(f)
-                if list(f) == [0, 1, 2]:
+                if list(f) == list(range(dim)):
                     continue
                 ok = True
                 for v in f:
@@ -102,10 +111,10 @@ def convexify_2d(points, vals, regions):
                     if b[v] == 0:
                         ok = False
                         break
-                if ok and _lower_normal(g[f])[2] < -TOL:
+                if ok and _lower_normal(g[f])[-1] < -TOL:
                     keep.append(f)
-            faces[i].append(np.array(keep, dtype=np.int64).reshape(-1, 3) if keep
-                            else np.arange(3)[None])
+            faces[i].append(np.array(keep, dtype=np.int64).reshape(-1, dim) if keep
+                            else np.arange(dim)[None])
             base[i, reg] = b[:nsub] == 1
     return base, faces
 
@@ -120,4 +129,4 @@ def piecewise_convexify(points, vals, regions):
                 [[np.arange(ndim + 1)[None]] * nregions for _ in range(nfuns)])
     if ndim == 1:
         return convexify_1d(points, vals, regions)
-    return convexify_2d(points, vals, regions)
+    return convexify_nd(points, vals, regions)

@@ -27,7 +27,12 @@ def rotation(rng, ndim):
     if ndim == 1:
         return np.ones((1, 1))
     phi = rng.random()
-    return np.array([[np.cos(phi), -np.sin(phi)], [np.sin(phi), np.cos(phi)]])
+    if ndim == 2:
+        return np.array([[np.cos(phi), -np.sin(phi)], [np.sin(phi), np.cos(phi)]])
+    u = rng.random(3)
+    u /= np.linalg.norm(u)
+    K = np.array([[0, -u[2], u[1]], [u[2], 0, -u[0]], [-u[1], u[0], 0]])
+    return np.eye(3) + np.sin(phi) * K + (1 - np.cos(phi)) * K @ K      # Rodrigues' formula
 
 
 def check_invariant(points, vals, regions, result, seed=0):
@@ -71,7 +76,7 @@ def test_handcrafted_2d():
     assert {tuple(f) for f in faces[0][0]} == {(0, 1, 5), (0, 2, 5), (1, 4, 5), (2, 4, 5)}
 
 
-@pytest.mark.parametrize("ndim", [1, 2])
+@pytest.mark.parametrize("ndim", [1, 2, 3])
 @pytest.mark.parametrize("fun", ["zero", "square"])
 def test_convex_functions(ndim, fun):
     """tests/convexhull.py:59-64: on a barycentric grid of the simplex a
@@ -121,6 +126,33 @@ def test_2d_matches_qhull_oracle(seed):
 
 
 @pytest.mark.parametrize("seed", range(4))
+def test_3d_matches_qhull_oracle(seed):
+    """3-D points: two tetrahedra sharing a face, interior points; the
+    oracle is the reference's own procedure with Qhull, which the reference
+    itself uses for 3-D points."""
+    rng = np.random.default_rng(100 + seed)
+    corners = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0],
+                        [1.0, 1.0, 1.0]])
+    tets = [(0, 1, 2, 3), (1, 2, 3, 4)]
+    npts = int(rng.integers(2, 9))
+    points, regions, off = [corners], [], len(corners)
+    for t in tets:
+        points.append(rng.dirichlet(np.ones(4), size=npts) @ corners[list(t)])
+        regions.append(list(t) + list(range(off, off + npts)))
+        off += npts
+    points, regions = np.concatenate(points), np.array(regions, dtype=np.int64)
+    vals = rng.standard_normal((5, points.shape[0]))
+    vals[::2] += 3.0 * (points ** 2).sum(axis=1)
+    vals[3] = -1.5
+    b1, f1 = ocvx.piecewise_convexify(points, vals, regions)
+    b2, f2 = piecewise_convexify(points, vals, regions)
+    np.testing.assert_array_equal(b1, b2)
+    for i in range(vals.shape[0]):
+        for j in range(2):
+            assert ({tuple(sorted(f)) for f in f1[i][j]} == {tuple(sorted(f)) for f in f2[i][j]})
+
+
+@pytest.mark.parametrize("seed", range(4))
 def test_1d_matches_oracle(seed):
     rng = np.random.default_rng(seed)
     L, S = 6, int(rng.integers(3, 9))
@@ -153,8 +185,8 @@ def test_threads_agree_and_simplex_regions():
         np.testing.assert_array_equal(a, b)
     base, faces = piecewise_convexify(points, vals, regions[:, :3])
     assert base.all() and all(np.array_equal(f, [[0, 1, 2]]) for fi in faces for f in fi)
-    with pytest.raises(NotImplementedError):
-        piecewise_convexify(np.zeros((4, 3)), np.zeros((1, 4)), np.array([[0, 1, 2, 3, 0]]))
+    base, faces = piecewise_convexify(rng.random((4, 3)), rng.random((2, 4)), np.array([[0, 1, 2, 3]]))
+    assert base.all() and all(np.array_equal(f, [[0, 1, 2, 3]]) for fi in faces for f in fi)
 
 
 def test_errors():
