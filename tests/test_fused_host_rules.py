@@ -1,10 +1,12 @@
-"""CPU checks of the batched solve's work list (`opyx_rof_batch_describe`, host
-code of libopyx): the sizing call, every pixel of every active instance in
-exactly one work item, items of one instance consecutive and in one tile-width
-class, tiles of equal width (a multiple of 4) in the class that leaves the
-fewest lanes idle, inactive instances without items, and the argument errors.
-No device memory is touched: the buffers are aligned placeholder addresses
-that the host code only copies."""
+"""CPU checks of the fused path's host-side rules in libopyx.
+
+The batched solve's work list (`opyx_rof_batch_describe`): the sizing call,
+every pixel of every active instance in exactly one work item, items of one
+instance consecutive and in one tile-width class, tiles of equal width (a
+multiple of 4) in the class that leaves the fewest lanes idle, inactive
+instances without items, and the argument errors.  The single-sweep
+selection (`opyx_rof_uses_sweep`).  No device memory is touched: the buffers
+are aligned placeholder addresses that the host code only copies."""
 
 import ctypes as C
 
@@ -138,3 +140,54 @@ def test_argument_errors(lib):
     probs, bufs = problems([(8, 130)])
     assert lib.opyx_rof_batch_describe(probs, bufs, 1, rec, None, 8, None, 0,
                                        C.byref(n)) == _lib.OPYX_ERR_ARG
+
+
+def _one(ndim, dims, C_=1, steps=2, dtype=None, y2=True):
+    p = _lib.opyx_rof_problem()
+    p.dtype = _lib.OPYX_F32 if dtype is None else dtype
+    p.ndim, p.nchannels, p.steps = ndim, C_, steps
+    for t, n in enumerate(dims):
+        p.dims[t], p.h[t] = n, 1.0
+    for k in range(C_):
+        p.weights[k] = p.vol[k] = 1.0
+    p.lbd, p.theta, p.tau, p.sigma = 0.1, 1.0, 0.3, 0.3
+    p.alpha0, p.eta, p.Delta = 0.5, 0.95, 1.5
+    b = _lib.opyx_rof_buffers()
+    a = 1 << 40
+    b.x, b.xbar, b.y, b.f, b.ws = a, a + (1 << 30), a + (2 << 30), a + (3 << 30), a + (4 << 30)
+    b.xgrad, b.gp = a + (5 << 30), a + (6 << 30)
+    if y2:
+        b.y2 = a + (7 << 30)
+    return p, b
+
+
+SWEEP_CASES = [
+    (dict(ndim=2, dims=(64, 128)), 1),
+    (dict(ndim=2, dims=(64, 128), C_=3), 1),
+    (dict(ndim=2, dims=(64, 128), steps=0), 1),                   # constant steps
+    (dict(ndim=2, dims=(64, 128), steps=1), 0),                   # adaptive: two passes and R
+    (dict(ndim=2, dims=(64, 128), dtype=_lib.OPYX_F64), 0),
+    (dict(ndim=2, dims=(64, 128), y2=False), 0),                  # no ping-pong buffer for y
+    (dict(ndim=2, dims=(64, 130)), 0),                            # rows not in quads
+    (dict(ndim=3, dims=(16, 32, 256)), 1),
+    (dict(ndim=3, dims=(16, 32, 128)), 1),
+    (dict(ndim=3, dims=(16, 32, 512)), 1),
+    (dict(ndim=3, dims=(16, 32, 64)), 0),                         # other row lengths: two passes
+    (dict(ndim=3, dims=(16, 32, 256), C_=2), 0),                  # several channels: two passes
+    (dict(ndim=1, dims=(4096,)), 0),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SWEEP_CASES)))
+def test_single_sweep_selection(lib, case):
+    """opyx_rof_uses_sweep (host code): the single sweep runs for FP32 with
+    constant or preconditioned steps and a y2 buffer -- 2-D, or 3-D with one
+    channel and rows of 128, 256 or 512 pixels, unmasked."""
+    kw, want = SWEEP_CASES[case]
+    p, b = _one(**kw)
+    assert lib.opyx_rof_uses_sweep(C.byref(p), C.byref(b)) == want
+    if kw["ndim"] == 3 and want:
+        b.mask = (1 << 40) + (8 << 30)
+        assert lib.opyx_rof_uses_sweep(C.byref(p), C.byref(b)) == 0
+    b.y2 = (b.y2 or 0) + 4                                          # misaligned y2
+    assert lib.opyx_rof_uses_sweep(C.byref(p), C.byref(b)) == 0
