@@ -462,6 +462,15 @@ def ssn_case(a, newton_steps=3):
                     "per CG iteration read by the host), Armijo search"}
 
 
+def guarded(case, a):
+    """One extra workload's record, or the error that stopped it: the
+    headline line does not depend on the other configurations."""
+    try:
+        return case(a)
+    except Exception as err:          # noqa: BLE001
+        return {"error": "%s: %s" % (type(err).__name__, str(err)[:300])}
+
+
 def e2e_solve(a, f):
     """The public-API call a user makes, host data in and out."""
     from opymize_gb300.functionals import SSD, HuberL1Norms
@@ -625,11 +634,11 @@ def run_gpu_arm(a, world, rank, local):
         if world == 1 and not a.no_extra:
             # the other configurations of the path, outside the headline metric
             del rs
-            out["other_workloads"] = {"volume_256x256x256": volume_case(a),
-                                      "sublabel_512x512_L16": sublabel_case(a),
-                                      "batched_512_instances": batch_case(a),
-                                      "warm_start_512x512": warm_start_case(a),
-                                      "semismooth_newton_256x256": ssn_case(a)}
+            out["other_workloads"] = {"volume_256x256x256": guarded(volume_case, a),
+                                      "sublabel_512x512_L16": guarded(sublabel_case, a),
+                                      "batched_512_instances": guarded(batch_case, a),
+                                      "warm_start_512x512": guarded(warm_start_case, a),
+                                      "semismooth_newton_256x256": guarded(ssn_case, a)}
         if world == 1 and not a.no_cpu:
             cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs_iters)
             out["cpu_baseline"] = {
