@@ -59,13 +59,14 @@ def parse():
 
 
 def workload_config(a, world):
+    ws_mb = 4 * a.size * a.size * a.channels * 7 // 2 ** 20
     return {
         "workload": "colour Huber-TV ROF %dx%dx%d fp32, alpha=%g, lambda=%g, precond steps, "
                     "until relgap<=%g" % (a.size, a.size, a.channels, a.huber, a.lbd, a.tol),
         "image": [a.size, a.size, a.channels], "lambda": a.lbd, "huber_alpha": a.huber,
         "steps": "precond", "tol": a.tol, "gap_check_every": a.gran, "seed": a.seed,
-        "l2": "working set (x, xbar, y, y2, f = %d MB) larger than L2 (126 MB)" %
-              (4 * a.size * a.size * a.channels * 7 // 2 ** 20),
+        "l2": "working set (x, xbar, y, y2, f = %d MB) %s than L2 (126 MB)" %
+              (ws_mb, "larger" if ws_mb > 126 else "smaller"),
         "parallelism": "replicas x%d" % world,
     }
 
@@ -250,6 +251,85 @@ def volume_case(a):
             "data": "synthetic ellipsoids, resident in HBM"}
 
 
+def gray_case(a, size=2048, lbd=0.1, gran=10, cpu_iters=20):
+    """Plain gray ROF (the reference example's model, examples/rof.py:60-80,
+    with its preconditioned steps): size^2, one channel, SSD + lambda*L1Norms
+    of the forward gradient, lambda = 0.1, noise 0.1, until relgap <= 1e-4
+    (gap every `gran` iterations), data resident; the public API from host
+    data; the one-channel sweep's share of the roofline; and the oracle on
+    the host cores (its set-up and one gap timed once, `cpu_iters`
+    iterations timed without set-up, scaled to the solve's counts)."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    from opymize_gb300.functionals import SSD, L1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG
+    t = torch()
+    dims = (size, size)
+    N = size * size
+    f = piecewise_constant(dims, 1, sigma=0.1, seed=a.seed)
+    rs = ResidentSolver(a, f, dims=dims, lbd=lbd, huber=0.0, gran=gran)
+    rs.solve(maxiter=100000)
+    e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    reps = 3
+    t.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        rs.solve(maxiter=100000)
+    e1.record()
+    t.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    iters = rs.iters
+    sw_bytes = 4.0 * N * (3 + 2 * 2)
+    tS = rs.time_pass(3)
+    peak = measured_peaks().get("hbm_gbs")
+    del rs
+    # the public API, host data in and out
+    s = PDHG(SSD(f.reshape(N, 1)), L1Norms(N, (1, 2), lbd), GradientOp(dims, 1, scheme="forward"))
+    s.solve(steps="precond", precision="float", term_pd_gap=a.tol, granularity=gran,
+            term_maxiter=100000)
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = PDHG(SSD(f.reshape(N, 1)), L1Norms(N, (1, 2), lbd), GradientOp(dims, 1, scheme="forward"))
+    s.solve(steps="precond", precision="float", term_pd_gap=a.tol, granularity=gran,
+            term_maxiter=100000)
+    x, y = s.state
+    t.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    rec = {"workload": "gray TV ROF %dx%d fp32, lambda=%g, precond steps, until relgap<=%g"
+                       % (size, size, lbd, a.tol),
+           "time_to_gap_ms": round(ms, 3), "iters_to_gap": iters,
+           "e2e_ms": round(e2e_ms, 3),
+           "sweep_us": round(tS * 1e6, 2), "sweep_GBps": round(sw_bytes / tS / 1e9, 1),
+           "sweep_frac_of_measured_hbm": round(sw_bytes / tS / 1e9 / peak, 3) if peak else None,
+           "sweep_algorithmic_bytes": sw_bytes,
+           "data": "synthetic piecewise-constant image + noise 0.1, resident in HBM"}
+    if not a.no_cpu:
+        so = cpu_solver(a, f, dims=dims, lbd=lbd, huber=0.0)
+        t0 = time.perf_counter()
+        so._setup()
+        t_setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        so.iterate(cpu_iters)
+        t_it = (time.perf_counter() - t0) / cpu_iters
+        t0 = time.perf_counter()
+        so.pd_gap()
+        t_gap = time.perf_counter() - t0
+        so.close()
+        cpu_ms = (t_setup + t_it * iters + t_gap * (iters // gran)) * 1e3
+        rec["cpu_baseline"] = {
+            "value": round(cpu_ms, 1), "unit": "ms", "cores": so.threads, "kind": "port",
+            "sample": "oracle (numpy/scipy port of the reference CPU PDHG, FP64) on the same "
+                      "input over %d host threads: set-up (%.3f s) and one gap (%.3f s) timed "
+                      "once, %d iterations timed without set-up (%.4f s/it), scaled to the "
+                      "solve's %d iterations and %d checks" % (so.threads, t_setup, t_gap,
+                                                               cpu_iters, t_it, iters,
+                                                               iters // gran)}
+        rec["cpu_over_gpu"] = round(cpu_ms / ms, 1)
+        rec["cpu_over_gpu_e2e"] = round(cpu_ms / e2e_ms, 1)
+    return rec
+
+
 def sublabel_case(a, iters=200):
     """The sublabel-lifted configuration: 512^2, 16 labels on [0, 1],
     rho = min((u - f)^2, 0.04) sampled at 8 points per interval, 10%
@@ -280,24 +360,39 @@ def sublabel_case(a, iters=200):
             "note": "wall time of solve() incl. setup of steps and one final gap"}
 
 
-def batch_case(a):
-    """The batched configuration: 512 independent 2-D instances, sides
-    log-uniform in [64, 1024], aspect U[0.5, 2], lambda U[0.02, 0.3], noise
-    sigma U[0.05, 0.2], FP32; every instance retires at its own relgap 1e-4;
-    rows per work item chosen by the autotuner (BatchROF)."""
-    from opymize_gb300.gpuarray import torch
-    from opymize_gb300.solvers import BatchROF
-    from opymize_gb300.tools.synthetic import piecewise_constant
-    t = torch()
-    rng = np.random.default_rng(a.seed)
-    imgs, lbds = [], []
-    for k in range(512):
+def batch_specs(seed, n=512):
+    """Sizes, noise levels and weights of the batched configuration's
+    instances (sides log-uniform in [64, 1024], aspect U[0.5, 2], lambda
+    U[0.02, 0.3], sigma U[0.05, 0.2])."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n):
         side = np.exp(rng.uniform(np.log(64), np.log(1024)))
         asp = rng.uniform(0.5, 2.0)
         H = max(8, int(round(side)))
         W = max(4, int(round(side * asp / 4)) * 4)
-        imgs.append(piecewise_constant((H, W), 1, sigma=rng.uniform(0.05, 0.2), seed=1000 + k))
-        lbds.append(rng.uniform(0.02, 0.3))
+        sigma = rng.uniform(0.05, 0.2)
+        lbd = rng.uniform(0.02, 0.3)
+        specs.append((H, W, sigma, lbd, 1000 + k))
+    return specs
+
+
+def batch_case(a, world=1, rank=0):
+    """The batched configuration: 512 independent 2-D instances, FP32; every
+    instance retires at its own relgap 1e-4; rows per work item and the check
+    interval chosen by the autotuner (BatchROF).  With several ranks the
+    instances are sharded by size (solvers.batch.shard, no collective on the
+    data path) and the per-instance stats gathered once at the end."""
+    from opymize_gb300.gpuarray import torch
+    from opymize_gb300.solvers import BatchROF
+    from opymize_gb300.solvers.batch import shard, gather_stats
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    t = torch()
+    specs = batch_specs(a.seed)
+    mine = shard([H * W for (H, W, _, _, _) in specs], rank, world)
+    imgs = [piecewise_constant((specs[i][0], specs[i][1]), 1, sigma=specs[i][2],
+                               seed=specs[i][4]) for i in mine]
+    lbds = [specs[i][3] for i in mine]
     b = BatchROF(imgs, lbds, tol=1e-4, granularity=None)   # rows per item and check interval tuned
     b.autotune()
     t.cuda.synchronize()
@@ -305,18 +400,24 @@ def batch_case(a):
     info = b.solve(maxiter=20000)
     t.cuda.synchronize()
     el = time.perf_counter() - t0
-    its = np.array([d["iter"] for d in info])
-    npx = np.array([im.shape[0] * im.shape[1] for im in imgs])
+    stats = {int(i): (int(d["iter"]), bool(d["converged"]), el) for i, d in zip(mine, info)}
+    merged = {}
+    for d in gather_stats(stats):
+        merged.update(d)
+    el = max(v[2] for v in merged.values())          # the slowest rank's wall time
+    its = np.array([merged[i][0] for i in range(len(specs))])
+    npx = np.array([H * W for (H, W, _, _, _) in specs])
     byts = float((28.0 * npx * its).sum())     # single sweep: 4 N (3C + 2K) bytes, C = 1, K = 2
     peak = measured_peaks().get("hbm_gbs")
     gbs = byts / el / 1e9
     return {"workload": "512 ROF instances, sides log-uniform [64, 1024], aspect U[0.5, 2], "
                         "lambda U[0.02, 0.3], sigma U[0.05, 0.2], fp32, retire at relgap 1e-4",
-            "solves_per_s": round(len(imgs) / el, 2), "wall_s": round(el, 3),
-            "converged": int(sum(d["converged"] for d in info)), "maxiter": 20000,
+            "ranks": world,
+            "solves_per_s": round(len(specs) / el, 2), "wall_s": round(el, 3),
+            "converged": int(sum(v[1] for v in merged.values())), "maxiter": 20000,
             "iters_median": float(np.median(its)), "iters_max": int(its.max()),
             "pixels": int(npx.sum()), "sum_bytes_per_wall_GBps": round(gbs, 1),
-            "frac_of_measured_hbm": round(gbs / peak, 3) if peak else None,
+            "frac_of_measured_hbm": round(gbs / peak / world, 3) if peak else None,
             "rows_per_item": b.rows_per_item, "granularity": b.gran,
             "tuning": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in b.tuning.items()},
             "launches": b.launches,
@@ -517,25 +618,15 @@ def profile_traffic():
     return out
 
 
-def cpu_sample(a, f, iters_to_gap, sample_iters=4):
-    """Oracle (CPU port of the reference, FP64) on the same input: time
-    `sample_iters` iterations and one gap evaluation, scale to the iteration
-    count of the solve."""
-    import oracle
-    n, C = a.size, a.channels
-    N = n * n
-    so = oracle.PDHG(oracle.SSD(f.reshape(N, C)), oracle.HuberL1Norms(N, (C, 2), a.lbd, a.huber),
-                     oracle.Gradient((n, n), C, "forward"))
+def cpu_sample(a, f):
+    """One whole solve of the oracle (CPU port of the reference, FP64, every
+    host thread) on the same input, wall clock: set-up, iterations, gaps."""
+    so = cpu_solver(a, f)
     t0 = time.perf_counter()
-    so.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=sample_iters,
-             granularity=sample_iters)
-    t_total = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    so.pd_gap()
-    t_gap = time.perf_counter() - t1
-    t_iter = (t_total - t_gap) / sample_iters
-    checks = iters_to_gap // a.gran
-    return (t_iter * iters_to_gap + t_gap * checks) * 1e3, t_iter, t_gap
+    info = so.solve(term_pd_gap=a.tol, term_maxiter=100000, granularity=a.gran)
+    dt = time.perf_counter() - t0
+    so.close()
+    return dt * 1e3, int(info["iter"]), so.threads
 
 
 def run_gpu_arm(a, world, rank, local):
@@ -613,8 +704,11 @@ def run_gpu_arm(a, world, rank, local):
         dist.all_reduce(v, op=dist.ReduceOp.MAX)
         e2e_ms = float(v.item())
 
+    # with several ranks the batched configuration is split across them (every
+    # rank takes part in the one gather of its stats)
+    batch_rec = guarded(lambda aa: batch_case(aa, world, rank), a) \
+        if world > 1 and not a.no_extra else None
     out = None
-    rs_iters = rs.iters
     if rank == 0:
         out = {
             "metric": METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world,
@@ -631,22 +725,25 @@ def run_gpu_arm(a, world, rank, local):
             "clocks": clocks,
             "gpu_launches": int(launches),
         }
+        if world > 1 and not a.no_extra:
+            out["other_workloads"] = {"batched_512_instances": batch_rec}
         if world == 1 and not a.no_extra:
             # the other configurations of the path, outside the headline metric
             del rs
-            out["other_workloads"] = {"volume_256x256x256": guarded(volume_case, a),
+            out["other_workloads"] = {"gray_2048x2048": guarded(gray_case, a),
+                                      "volume_256x256x256": guarded(volume_case, a),
                                       "sublabel_512x512_L16": guarded(sublabel_case, a),
                                       "batched_512_instances": guarded(batch_case, a),
                                       "warm_start_512x512": guarded(warm_start_case, a),
                                       "semismooth_newton_256x256": guarded(ssn_case, a)}
         if world == 1 and not a.no_cpu:
-            cpu_ms, t_iter, t_gap = cpu_sample(a, f, rs_iters)
+            cpu_ms, cpu_iters, thr = cpu_sample(a, f)
             out["cpu_baseline"] = {
-                "value": round(cpu_ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
-                "sample": "oracle PDHG (numpy/scipy port of the reference CPU path, FP64) on "
-                          "the same 2048x2048x3 input: 4 iterations (%.3f s/it) and one gap "
-                          "evaluation (%.3f s) timed, scaled to the %d iterations and %d gap "
-                          "checks of the solve" % (t_iter, t_gap, rs_iters, rs_iters // a.gran),
+                "value": round(cpu_ms, 1), "unit": UNIT, "cores": thr, "kind": "port",
+                "sample": "one whole solve of the oracle (numpy/scipy port of the reference CPU "
+                          "PDHG, FP64) on the same %dx%dx%d input from a zero start to relgap %g "
+                          "(%d iterations, gap every %d), array operations split over %d host "
+                          "threads" % (a.size, a.size, a.channels, a.tol, cpu_iters, a.gran, thr),
                 "host_cpus": os.cpu_count()}
     if dist:
         dist.barrier()
@@ -655,64 +752,75 @@ def run_gpu_arm(a, world, rank, local):
 
 
 # ------------------------------------------------------------ reference arm
+def cpu_solver(a, f, dims=None, lbd=None, huber=None):
+    """The oracle's PDHG (numpy/scipy port of the reference's CPU solver,
+    FP64) over every host thread (oracle.threaded: pixel ranges of each
+    array operation on a thread pool; same iterates as the one-thread port)."""
+    from oracle.threaded import ThreadedROF
+    dims = (a.size, a.size) if dims is None else tuple(dims)
+    return ThreadedROF(f.reshape(-1, f.shape[-1]), dims, a.lbd if lbd is None else lbd,
+                       a.huber if huber is None else huber)
+
+
 def run_reference_arm(a, world, rank):
+    """Each step is one whole CPU solve to the gap (set-up, iterations and
+    gap checks, as a caller of solve() sees it), timed on the wall clock."""
     if rank != 0:
         return None
-    import oracle
     f = make_image(a)
-    n, C = a.size, a.channels
-    N = n * n
-
-    def problem():
-        return oracle.PDHG(oracle.SSD(f.reshape(N, C)),
-                           oracle.HuberL1Norms(N, (C, 2), a.lbd, a.huber),
-                           oracle.Gradient((n, n), C, "forward"))
-
-    # one full CPU solve to the gap (untimed pass that fixes the iteration
-    # count; its wall time is reported as well)
-    so = problem()
-    t0 = time.perf_counter()
-    so.solve(steps="precond", term_pd_gap=a.tol, term_maxiter=100000, granularity=a.gran)
-    full_s = time.perf_counter() - t0
-    iters = int(so.info["iter"])
-    checks = iters // a.gran
-    sample = 2
-    samples = []
+    so = cpu_solver(a, f)
+    times, iters = [], None
     for k in range(a.warmup + a.steps):
-        sp = problem()
         t0 = time.perf_counter()
-        sp.solve(steps="precond", term_pd_gap=1e-300, term_maxiter=sample, granularity=sample)
-        t_it_gap = time.perf_counter() - t0
-        t1 = time.perf_counter()
-        sp.pd_gap()
-        t_gap = time.perf_counter() - t1
+        info = so.solve(term_pd_gap=a.tol, term_maxiter=100000, granularity=a.gran)
+        dt = time.perf_counter() - t0
+        iters = int(info["iter"])
         if k >= a.warmup:
-            samples.append(((t_it_gap - t_gap) / sample, t_gap))
-    t_iter = float(np.median([s[0] for s in samples]))
-    t_gap = float(np.median([s[1] for s in samples]))
-    ms = (t_iter * iters + t_gap * checks) * 1e3
+            times.append(dt)
+    so.close()
+    ms = float(np.mean(times)) * 1e3
     return {
         "metric": METRIC, "value": round(ms, 1), "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms, 1),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded piecewise-constant image + noise)",
         "config": workload_config(a, world), "impl": "reference",
-        "iters_to_gap": iters, "full_solve_ms": round(full_s * 1e3, 1),
-        "cpu_baseline": {"value": round(ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": "each step: %d iterations + 1 gap evaluation of the oracle "
-                                   "(numpy/scipy port of the reference CPU PDHG) on the full "
-                                   "input, scaled to the %d iterations / %d checks its own "
-                                   "untimed full solve needed (%.1f s)" % (sample, iters, checks,
-                                                                            full_s),
+        "iters_to_gap": iters, "final_relgap": info["relgap"],
+        "step_ms_min_max": [round(1e3 * min(times), 1), round(1e3 * max(times), 1)],
+        "cpu_baseline": {"value": round(ms, 1), "unit": UNIT, "cores": so.threads, "kind": "port",
+                         "sample": "each step: one whole solve of the oracle (numpy/scipy port of "
+                                   "the reference CPU PDHG, FP64) on the full input from a zero "
+                                   "start to relgap %g: set-up, %d iterations, %d gap checks; "
+                                   "array operations split over %d host threads"
+                                   % (a.tol, iters, iters // a.gran, so.threads),
                          "host_cpus": os.cpu_count()},
         "e2e": {"value": round(ms, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
 
 
+def relaunch_ranks(n):
+    """`bench.py --gpus N` started as one process: run it again as N ranks
+    (one per GPU) under torch.distributed.run on 127.0.0.1, and return their
+    exit status.  Rank 0 prints the line."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           "--nproc-per-node=%d" % n, "--master-addr=127.0.0.1", "--master-port=%d" % port,
+           os.path.abspath(__file__)] + sys.argv[1:]
+    env = dict(os.environ, MASTER_ADDR="127.0.0.1")
+    return subprocess.call(cmd, env=env)
+
+
 def main():
     a = parse()
+    if a.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_ranks(a.gpus))
     world, rank, local = dist_setup()
+    if "WORLD_SIZE" in os.environ and world != a.gpus:
+        raise SystemExit("bench.py: --gpus %d but WORLD_SIZE=%d" % (a.gpus, world))
     if a.impl == "reference":
         out = run_reference_arm(a, world, rank)
     else:

@@ -492,7 +492,12 @@ int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* part
  * OPYX_ERR_SCRATCH_LIMIT before any launch.  Each call starts a fresh
  * segment from the x, y it is given (step state from `p`), runs `iters`
  * iterations and, if `gap_out` (device double[6]) is not NULL, writes
- * objp, objd, infeasp, infeasd, gap, relgap there.  The first call on a
+ * objp, objd, infeasp, infeasd, gap, relgap there.  It always runs the
+ * two-pass iteration (pass A, pass B per iteration): the single sweep needs a
+ * second y buffer, which this entry point does not hold, so FP32 const and
+ * precond problems run at the two passes' speed rather than the sweep's.
+ * Dims whose product overflows (N * D * C above 2^40) also return
+ * OPYX_ERR_SCRATCH_LIMIT.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress); make
  * that first call before any stream capture.  All calls share the one
  * array: calls that overlap on the GPU (other streams, other threads) race. */

@@ -26,14 +26,35 @@ constexpr size_t kWsBytes = kTicketOff + 256;
 static_assert(sizeof(opyx_adaptive_state) <= 256, "state record too large");
 static_assert(sizeof(opyx_rof_info) <= 256, "info record too large");
 
+// Problems with more than 2^40 dual values (N * D * C) are rejected: far
+// beyond any device memory, and it keeps every product of the dims, the
+// channel count and an element size inside int64.
+constexpr int64_t kMaxValues = (int64_t)1 << 40;
+
+// N = prod(dims) for ndim in [1, 3] and nchannels in [1, OPYX_ROF_MAX_C];
+// false if a dim is < 1 or N * ndim * nchannels exceeds kMaxValues (checked
+// before each multiplication, so nothing wraps).
+static bool count_pixels(const opyx_rof_problem* p, int64_t* n_out) {
+  int64_t n = 1;
+  for (int t = 0; t < p->ndim; ++t) {
+    if (p->dims[t] < 1 || p->dims[t] > kMaxValues / n) return false;
+    n *= p->dims[t];
+  }
+  if (n > kMaxValues / ((int64_t)p->ndim * p->nchannels)) return false;
+  *n_out = n;
+  return true;
+}
+
 static int validate(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   if (!p || !b) return OPYX_ERR_ARG;
   if (p->dtype != OPYX_F32 && p->dtype != OPYX_F64) return OPYX_ERR_ARG;
   if (p->ndim < 1 || p->ndim > 3) return OPYX_ERR_UNSUPPORTED;
   if (p->nchannels < 1 || p->nchannels > OPYX_ROF_MAX_C) return OPYX_ERR_UNSUPPORTED;
   if (p->steps < OPYX_STEPS_CONST || p->steps > OPYX_STEPS_PRECOND) return OPYX_ERR_ARG;
+  int64_t npix = 0;
+  if (!count_pixels(p, &npix)) return OPYX_ERR_ARG;
   for (int t = 0; t < p->ndim; ++t)
-    if (p->dims[t] < 1 || !(p->h[t] > 0)) return OPYX_ERR_ARG;
+    if (!(p->h[t] > 0)) return OPYX_ERR_ARG;
   for (int k = 0; k < p->nchannels; ++k)
     if (!(p->vol[k] > 0)) return OPYX_ERR_ARG;
   if (!(p->lbd > 0) || p->huber_alpha < 0 || !(p->theta > 0)) return OPYX_ERR_ARG;
@@ -595,11 +616,10 @@ extern "C" int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void
   if (!p || iters < 0) return OPYX_ERR_ARG;
   if (p->ndim < 1 || p->ndim > 3 || p->nchannels < 1 || p->nchannels > OPYX_ROF_MAX_C)
     return OPYX_ERR_UNSUPPORTED;
-  int64_t N = 1;
-  for (int t = 0; t < p->ndim; ++t) {
+  for (int t = 0; t < p->ndim; ++t)
     if (p->dims[t] < 1) return OPYX_ERR_ARG;
-    N *= p->dims[t];
-  }
+  int64_t N = 0;
+  if (!count_pixels(p, &N)) return OPYX_ERR_SCRATCH_LIMIT;
   const size_t esz = p->dtype == OPYX_F64 ? 8 : 4;
   const size_t field = round256((size_t)N * p->nchannels * esz);
   const int nfields = p->steps == OPYX_STEPS_ADAPTIVE ? 3 : 1;   // xbar [, xgrad, gp]

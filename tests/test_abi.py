@@ -130,6 +130,24 @@ def _conv(**kw):
     return d
 
 
+def _rof(dims, C=1):
+    p = _lib.opyx_rof_problem()
+    p.dtype, p.ndim, p.nchannels, p.steps = _lib.OPYX_F32, len(dims), C, 2   # precond
+    for t, n in enumerate(dims):
+        p.dims[t], p.h[t] = n, 1.0
+    for k in range(C):
+        p.weights[k] = p.vol[k] = 1.0
+    p.lbd, p.theta = 0.1, 1.0
+    return p
+
+
+def _rof_buffers():
+    b = _lib.opyx_rof_buffers()
+    b.x, b.xbar, b.y, b.f, b.ws, b.y2 = _P, _P + 4096, _P + 8192, _P + 12288, _P + 65536, \
+        _P + 131072
+    return b
+
+
 ARG, UNSUP, WS, OK = (_lib.OPYX_ERR_ARG, _lib.OPYX_ERR_UNSUPPORTED, _lib.OPYX_ERR_WORKSPACE,
                       _lib.OPYX_OK)
 
@@ -159,6 +177,17 @@ ERROR_CASES = [
     ("opyx_conv3x3", (_conv(in_channels=24, in_stride=24), None), ARG),  # channels per chunk
     ("opyx_conv3x3", (_conv(out_channels=48, out_stride=48), None), UNSUP),
     ("opyx_conv3x3", (_conv(x=_P + 8), None), ARG),                    # 16-byte alignment
+    # dims whose product wraps int64 ({2^62 + 1, 4} would wrap to 4 pixels)
+    ("opyx_rof_init", (_rof((2 ** 62 + 1, 4)), _rof_buffers(), None), ARG),
+    ("opyx_rof_iterate", (_rof((2 ** 62 + 1, 4)), _rof_buffers(), 1, None), ARG),
+    ("opyx_rof_init", (_rof((2 ** 21, 2 ** 21, 2 ** 21)), _rof_buffers(), None), ARG),
+    ("opyx_rof_init", (_rof((2 ** 20, 2 ** 19), C=4), _rof_buffers(), None), ARG),  # > 2^40 values
+    ("opyx_rof_init", (_rof((0, 4)), _rof_buffers(), None), ARG),
+    ("opyx_rof_iterate_noalloc", (_rof((2 ** 62 + 1, 4)), _P, _P, _P, None, 1, None, None),
+     _lib.OPYX_ERR_SCRATCH_LIMIT),
+    ("opyx_rof_iterate_noalloc", (_rof((4096, 4096)), _P, _P, _P, None, 1, None, None),
+     _lib.OPYX_ERR_SCRATCH_LIMIT),                                     # xbar does not fit
+    ("opyx_rof_iterate_noalloc", (_rof((0, 4)), _P, _P, _P, None, 1, None, None), ARG),
 ]
 
 

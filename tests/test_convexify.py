@@ -243,3 +243,26 @@ def test_degenerate_inputs():
 
 def test_reference_module_path():
     assert piecewise_convexify_ref_path is piecewise_convexify
+
+
+def test_1d_three_point_intervals():
+    """1-D regions of three points take the gift-wrap path, as in the
+    reference, whose only shortcut for them is the bare-simplex case
+    nsub == ndim + 1 (quickhull/__init__.pyx:30); its nd-path test
+    nsubpoints == 3 (:116) is never reached for ndim 1.  Expected masks
+    follow getConvexHull1D (quickhull/convexhull.cpp:190-217): from each hull
+    point the next one is the smallest rounded slope, ties to the farthest."""
+    points = np.array([[0.0], [0.5], [1.0], [1.5], [2.0], [7.0]])   # point 5 in no region
+    regions = np.array([[0, 2, 1], [2, 4, 3]], dtype=np.int64)       # endpoints first
+    vals = np.array([[0.0, 1.0, 0.0, -1.0, 0.0, 3.0],    # middle above its chord: dropped;
+                                                          # below: kept
+                     [0.0, 0.5, 1.0, 1.5, 2.0, 3.0]])     # collinear: ties to the farthest
+    want = np.array([[1, 0, 1, 1, 1, 0],
+                     [1, 0, 1, 0, 1, 0]], dtype=bool)
+    for fn in (piecewise_convexify, ocvx.piecewise_convexify):
+        base, faces = fn(points, vals, regions)
+        np.testing.assert_array_equal(base, want)
+    _, faces = piecewise_convexify(points, vals, regions)
+    assert sorted(map(tuple, faces[0][0])) == [(0, 1)]            # positions in regions[0]
+    assert sorted(map(tuple, faces[0][1])) == [(0, 2), (2, 1)]
+    assert sorted(map(tuple, faces[1][1])) == [(0, 1)]

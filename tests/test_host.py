@@ -87,3 +87,23 @@ def test_batch_check_interval():
     for t_gap in np.geomspace(1e-3, 10.0, 40):
         g = BatchROF.check_interval(t_gap, 0.37)
         assert g % 2 == 0 and 10 <= g <= 100
+
+
+def test_interrupt_handler_first_sigint_recorded_second_raises():
+    """A solve's first Ctrl-C is recorded (the loop stops at its next check);
+    the handler installed before is back at once, so a second one raises."""
+    import os
+    import signal
+    import time
+    from opymize_gb300.tools.util import GracefulInterruptHandler
+    before = signal.getsignal(signal.SIGINT)
+    with GracefulInterruptHandler() as h:
+        assert not h.interrupted
+        os.kill(os.getpid(), signal.SIGINT)
+        time.sleep(0.01)
+        assert h.interrupted
+        assert signal.getsignal(signal.SIGINT) is before
+        with pytest.raises(KeyboardInterrupt):
+            os.kill(os.getpid(), signal.SIGINT)
+            time.sleep(0.01)
+    assert signal.getsignal(signal.SIGINT) is before
