@@ -174,10 +174,15 @@ typedef struct {
   const int64_t* eq_off;      /* (nregions*nfuns + 1) row offsets, or NULL  */
   const double* eqns;         /* (eq_off[last], ndim+1), or NULL            */
   const double* checks;       /* (nregions, ndim+1, ndim+1), or NULL        */
+  const void* bt;             /* (npoints, nfuns) copy of b, or NULL: ndim 1
+                                 projections read it coalesced              */
+  const uint8_t* It;          /* (npoints, nfuns) copy of I, or NULL        */
 } opyx_epigraph;
 
 /* y = EpigraphProj(x) (proj.py:388-480; reference kernel `epigraphproj` with
- * `solve_qp`, proj.cu:660-831): per-instance active-set QP.  y may equal x.
+ * `solve_qp`, proj.cu:660-831): per-instance active-set QP; for ndim 1 with
+ * at most 16 points per region the exact projection onto the piecewise-
+ * linear epigraph's pieces in one pass instead.  y may equal x.
  * Instances whose QP did not finish within maxiter steps (the reference uses
  * ndim*nsubpoints, tolerance 1e-9) are counted into *nonconv (device
  * unsigned, may be NULL); the reference prints a warning instead. */

@@ -75,7 +75,8 @@ class opyx_epigraph(C.Structure):
     _fields_ = [("ndim", C.c_int32), ("nsubpoints", C.c_int32), ("nfuns", C.c_int64),
                 ("nregions", C.c_int64), ("npoints", C.c_int64), ("I", C.c_void_p),
                 ("J", C.c_void_p), ("v", C.c_void_p), ("b", C.c_void_p),
-                ("eq_off", C.c_void_p), ("eqns", C.c_void_p), ("checks", C.c_void_p)]
+                ("eq_off", C.c_void_p), ("eqns", C.c_void_p), ("checks", C.c_void_p),
+                ("bt", C.c_void_p), ("It", C.c_void_p)]
 
 
 class opyx_rof_problem(C.Structure):

@@ -367,6 +367,81 @@ k_proj(opyx_epigraph e, const T* __restrict__ x, T* y, int maxiter, double tol,
   if (nonconv && bad) atomicAdd(nonconv, bad);
 }
 
+// ndim = 1 with at most kDirect constraints per instance: the exact
+// projection in one pass, no iterations.  The constraints bound the
+// epigraph of g(s) = max_l (v_l s - b_l), a convex piecewise-linear function
+// of one variable; line l is the graph of g on [lo_l, hi_l] with
+//   lo_l = max over v_m < v_l of (b_l - b_m) / (v_l - v_m),
+//   hi_l = min over v_m > v_l of (b_l - b_m) / (v_l - v_m)
+// (no piece if lo_l > hi_l, or if a line of the same slope lies below it;
+// of two equal lines the first counts).  A point (s0, t0) below the graph
+// projects onto the nearest piece: the orthogonal projection onto line l,
+// s = (s0 + v_l (t0 + b_l)) / (1 + v_l^2), clamped to [lo_l, hi_l].  Points
+// with no positive violation are kept, as by the active-set method.  The
+// result is the QP's solution up to rounding, so instances never count as
+// not converged.  Optional transposed copies bt (npoints, nfuns) of b and
+// It of I make the reads of neighbouring instances (consecutive i)
+// coalesced.
+constexpr int kDirect = 16;
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(kThreads)
+k_proj1(opyx_epigraph e, const T* __restrict__ x, T* y) {
+  const int64_t total = e.nregions * e.nfuns;
+  const T* v = (const T*)e.v;
+  const T* b = (const T*)e.b;
+  const T* bt = (const T*)e.bt;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / e.nfuns, i = t - j * e.nfuns;
+    const T s0 = x[2 * t], t0 = x[2 * t + 1];
+    T cv[NS], cb[NS];
+    bool on[NS];
+    T viol = T(0);
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const bool used = k < e.nsubpoints;
+      const int64_t l = used ? e.J[j * e.nsubpoints + k] : 0;
+      on[k] = used && (e.It ? e.It[l * e.nfuns + i] : e.I[i * e.npoints + l]) != 0;
+      cv[k] = on[k] ? v[l] : T(0);
+      cb[k] = on[k] ? (bt ? bt[l * e.nfuns + i] : b[i * e.npoints + l]) : T(0);
+      if (on[k]) {
+        const T r = cv[k] * s0 - t0 - cb[k];
+        if (!any || r > viol) viol = r;
+        any = true;
+      }
+    }
+    T ys = s0, yt = t0;
+    if (any && viol > T(0)) {
+      T best = T(INFINITY);
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        if (!on[k]) continue;
+        T lo = -T(INFINITY), hi = T(INFINITY);
+        bool live = true;
+#pragma unroll
+        for (int m = 0; m < NS; ++m) {
+          if (m == k || !on[m]) continue;
+          const T dv = cv[k] - cv[m];
+          const T db = cb[k] - cb[m];
+          if (dv > T(0)) lo = fmax(lo, db / dv);
+          else if (dv < T(0)) hi = fmin(hi, db / dv);
+          else if (db > T(0) || (db == T(0) && m < k)) live = false;
+        }
+        if (!live || lo > hi) continue;
+        T s = (s0 + cv[k] * (t0 + cb[k])) / (T(1) + cv[k] * cv[k]);
+        s = fmin(fmax(s, lo), hi);
+        const T tt = cv[k] * s - cb[k];
+        const T d = (s - s0) * (s - s0) + (tt - t0) * (tt - t0);
+        if (d < best) { best = d; ys = s; yt = tt; }
+      }
+    }
+    y[2 * t] = ys;
+    y[2 * t + 1] = yt;
+  }
+}
+
 // which = 0: EpigraphInd (val 0, infeas = max(0, max_l a_l.x - b_l));
 // which = 1: EpigraphSupp (val = sum xt * max_f <eq_f, (x[:n]/xt, 1)>, xt =
 // max(eps, |x[n]|); infeas = max(0, -checks[j] x)) (epigraph.py:40-46, :101-112).
@@ -508,6 +583,17 @@ int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y
                                                         tol, nonconv)                     \
        : k_proj<TT, ND, 0><<<g, kThreads, 0, s>>>(*e, (const TT*)x, (TT*)y, maxiter, tol,  \
                                                   nonconv))
+  if (e->ndim == 1 && e->nsubpoints <= kDirect && (dtype == OPYX_F32 || dtype == OPYX_F64)) {
+    // the direct projection (exact, no iterations)
+    if (dtype == OPYX_F32) {
+      if (e->nsubpoints <= 8) k_proj1<float, 8><<<g, kThreads, 0, s>>>(*e, (const float*)x, (float*)y);
+      else k_proj1<float, kDirect><<<g, kThreads, 0, s>>>(*e, (const float*)x, (float*)y);
+    } else {
+      if (e->nsubpoints <= 8) k_proj1<double, 8><<<g, kThreads, 0, s>>>(*e, (const double*)x, (double*)y);
+      else k_proj1<double, kDirect><<<g, kThreads, 0, s>>>(*e, (const double*)x, (double*)y);
+    }
+    return check_launch();
+  }
   if (dtype == OPYX_F32) {
     if (e->ndim == 1) OPYX_EPI_LAUNCH(float, 1);
     else if (e->ndim == 2) OPYX_EPI_LAUNCH(float, 2);

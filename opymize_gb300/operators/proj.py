@@ -205,18 +205,27 @@ class _EpigraphData(object):
         self._ij = None
 
     def struct(self, dtype, supp=None):
+        # ndim 1 projections read transposed copies of I and b (instances of
+        # one region with consecutive functions read consecutive values)
+        tr = self.ndim == 1
         if self._ij is None:
             self._ij = (DeviceArray.to_gpu(np.ascontiguousarray(self.I, dtype=np.uint8)),
-                        DeviceArray.to_gpu(np.ascontiguousarray(self.J, dtype=np.int64)))
+                        DeviceArray.to_gpu(np.ascontiguousarray(self.J, dtype=np.int64)),
+                        DeviceArray.to_gpu(np.ascontiguousarray(self.I.T, dtype=np.uint8))
+                        if tr else None)
         key = np.dtype(dtype).str
         if key not in self._dev:
             self._dev[key] = (DeviceArray.to_gpu(np.ascontiguousarray(self.v), dtype),
-                              DeviceArray.to_gpu(np.ascontiguousarray(self.b), dtype))
+                              DeviceArray.to_gpu(np.ascontiguousarray(self.b), dtype),
+                              DeviceArray.to_gpu(np.ascontiguousarray(self.b.T), dtype)
+                              if tr else None)
         e = _lib.opyx_epigraph()
         e.ndim, e.nsubpoints = self.ndim, self.nsubpoints
         e.nfuns, e.nregions, e.npoints = self.nfuns, self.nregions, self.npoints
         e.I, e.J = self._ij[0].ptr, self._ij[1].ptr
         e.v, e.b = self._dev[key][0].ptr, self._dev[key][1].ptr
+        if tr:
+            e.It, e.bt = self._ij[2].ptr, self._dev[key][2].ptr
         if supp is not None:
             e.eq_off, e.eqns, e.checks = (None if a is None else a.ptr for a in supp)
         return e
@@ -232,7 +241,9 @@ class EpigraphProj(Operator):
     reference's GPU method, proj.cu:660-790); the iteration bound and the
     tolerance are the reference's (ndim*nsubpoints, 1e-9).  Instances that
     hit the bound keep their last iterate and are counted in
-    ``nonconverged`` (the reference prints a warning)."""
+    ``nonconverged`` (the reference prints a warning).  For ndim 1 with at
+    most 16 points per region the same projection is computed directly: the
+    nearest of the epigraph boundary's line pieces, no iterations."""
 
     def __init__(self, I, J, v, b, Ab=None):
         Operator.__init__(self)

@@ -95,3 +95,38 @@ def test_ssn_reaches_a_tight_gap_from_pdhg():
     info = s.solve(continue_at=p.state, granularity=5, term_relgap=1e-300, term_maxiter=5)
     assert all(np.isfinite(v).all() for v in s.state)
     assert abs(info["relgap"]) <= 1.01 * abs(p.info["relgap"]) + 1e-12
+
+
+def test_ssn_ten_steps_follow_the_oracle():
+    """Ten Newton steps from a PDHG start (48 x 40 gray, lambda 0.1), device
+    against the oracle's restatement of the reference's solver, and the
+    progress both make.  The reference's method barely moves from a PDHG
+    point: its CG stops once |r|^2 falls below the current residual
+    0.5 |R|^2 (semismooth_newton.py:77-117), so its steps are inexact, and
+    0.5 |R|^2 drops by well under 5 % in 10 steps (the oracle shows the same
+    over 40 steps).  The device solver matches that trajectory rather than
+    improving on it."""
+    import oracle
+    from oracle.ssn import SemismoothNewton as OracleSSN
+    from opymize_gb300.functionals import SSD, L1Norms
+    from opymize_gb300.linear import GradientOp
+    from opymize_gb300.solvers import PDHG, SemismoothNewton
+    from opymize_gb300.tools.synthetic import piecewise_constant
+    dims = (48, 40)
+    N = int(np.prod(dims))
+    f = piecewise_constant(dims, 1, sigma=0.1, seed=3).reshape(N, 1)
+    p = PDHG(SSD(f), L1Norms(N, (1, 2), 0.1), GradientOp(dims, 1))
+    p.solve(steps="precond", precision="double", term_pd_gap=1e-300, term_maxiter=500,
+            granularity=500)
+    start = np.concatenate([v.ravel() for v in p.state])
+    np.random.seed(1)
+    s = SemismoothNewton(SSD(f), L1Norms(N, (1, 2), 0.1), GradientOp(dims, 1))
+    s.solve(continue_at=start.copy(), granularity=10, term_relgap=1e-300, term_maxiter=10)
+    xy = np.concatenate([v.ravel() for v in s.state])
+    o = OracleSSN(f, 0.1, oracle.Gradient(dims, 1, "centered"), 2)
+    ref = o.solve(start, 10)
+    assert rel(xy, ref) < 1e-6, rel(xy, ref)
+    res = np.zeros_like(start)
+    r0, r10 = o._res(start, res), o._res(xy, res)
+    assert r10 < r0                       # it descends ...
+    assert r10 > 0.95 * r0                # ... by little, as the reference does
