@@ -484,6 +484,32 @@ int opyx_rof_batch_iterate_class(const void* host_desc, const void* dev_desc, in
 int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* partials,
                        void* stream);
 
+/* Persistent batched solve of one-channel instances with constant or
+ * preconditioned steps (all alike): ONE cooperative launch runs `maxiter`
+ * (even) iterations of every instance of the descriptor, checks the gap of
+ * the active ones every `gran` (even) iterations and retires each instance
+ * at its own stop test (the reference's per-solve loop, pdhg.py:287-305,
+ * for every instance of the batch; each reference solve is one PDHG
+ * object).  Work items are strips of 128 pixels by runs of rows_per_item
+ * rows (the descriptor's), taken by warps from a counter every iteration;
+ * a grid barrier separates the iterations.  Iterates equal those of the
+ * single-image solve bit for bit.  ws: device memory of
+ * opyx_rof_batch_persist_ws_bytes(host_desc) bytes, 256-byte aligned; it
+ * starts with the control record opyx_rof_persist_ctl (cleared by the call;
+ * after the launch `error` != 0 means a barrier timed out -- every wait is
+ * bounded -- `nact`/`nwork` are the instances / strips still active and
+ * `iters` the iterations at the last check).  Call opyx_rof_batch_init
+ * first.  The info records hold each instance's objectives, check count
+ * and stop flag as for opyx_rof_batch_gap. */
+typedef struct {
+  uint64_t arrive;
+  uint32_t grab[4];
+  int32_t error, nact, nwork, iters;
+} opyx_rof_persist_ctl;
+size_t opyx_rof_batch_persist_ws_bytes(const void* host_desc);
+int opyx_rof_batch_persist(const void* host_desc, const void* dev_desc, void* ws, int gran,
+                           int maxiter, void* stream);
+
 /* Allocation-free variant of opyx_rof_init + opyx_rof_iterate (+ opyx_rof_gap).
  * It has no counterpart in the reference: it serves callers that cannot
  * allocate device memory (code running inside another framework's memory

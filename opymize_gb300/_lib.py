@@ -184,6 +184,8 @@ SIGNATURES = {
     "opyx_rof_batch_iterate": (i32, [vp, vp, i32, vp]),
     "opyx_rof_batch_iterate_class": (i32, [vp, vp, i32, i32, vp]),
     "opyx_rof_batch_gap": (i32, [vp, vp, vp, vp]),
+    "opyx_rof_batch_persist_ws_bytes": (sz, [vp]),
+    "opyx_rof_batch_persist": (i32, [vp, vp, vp, i32, i32, vp]),
     "opyx_conv3x3": (i32, [P(opyx_conv3x3_desc), vp]),
     "opyx_conv3x3_wgrad_workspace": (sz, [P(opyx_conv3x3_desc)]),
     "opyx_conv3x3_wgrad": (i32, [P(opyx_conv3x3_desc), vp, vp, i32, vp, sz, vp]),

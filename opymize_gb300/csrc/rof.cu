@@ -9,6 +9,7 @@
 #include "rof_pipe.cuh"
 #include "rof_sweep.cuh"
 #include "rof_sweep3.cuh"
+#include "rof_sweep1.cuh"
 
 namespace opyx {
 namespace rof {
@@ -678,6 +679,7 @@ constexpr size_t kBatchRecord = 512;   // [0, 256) step state, [256, 512) info
 // batch_tiles for the choice per image), so narrow images do not leave most
 // of a 512-pixel CTA idle; the sweep launches once per class.
 constexpr int kBatchClasses = 3;
+constexpr int kStripW = 128;   // pixels per work item of the persistent solve (one warp)
 constexpr int kBatchTW[kBatchClasses] = {128, 256, 512};
 
 // Column tiles of an instance with rows of nl pixels: n tiles of equal width
@@ -700,8 +702,9 @@ static int batch_tiles(int64_t nl, int64_t* tw) {
 }
 
 struct BatchHeader {
-  int32_t ninst, nitems, nchannels, pad;
+  int32_t ninst, nitems, nchannels, rows_per_item;
   int32_t class_beg[kBatchClasses + 1];   // items of class c: [class_beg[c], class_beg[c+1])
+  int32_t witems, pad;                    // strips of the persistent solve (all instances)
 };
 
 struct BatchInst {
@@ -710,6 +713,9 @@ struct BatchInst {
   opyx_adaptive_state st0;
   double ssd_shift;
   int32_t item_beg, item_end;
+  // the persistent solve's work items: strips of 128 pixels by runs of
+  // rows_per_item rows, w_ntx across and w_nty down, numbered from w_beg
+  int32_t w_beg, w_ntx, w_nty, w_pad;
 };
 
 struct BatchItem {
@@ -928,6 +934,267 @@ __global__ void k_batch_init(const BatchInst* __restrict__ insts, int ninst) {
   memset(info, 0, sizeof(opyx_rof_info));
 }
 
+// ---------------------------------------------------------------------------
+// Persistent batched solve (one channel): one cooperative launch runs every
+// iteration, gap check and retirement of the batch.  Each iteration, the
+// warps take work items -- strips of 128 pixels by runs of rows of the
+// active instances -- from a counter and sweep them (sweep_strip1); a grid
+// barrier ends the iteration.  Every `gran` iterations the warps write each
+// strip's partial gap sums, the CTAs fold each active instance's sums into
+// its info record with the reference's stop test (pdhg.py:287-305), and CTA
+// 0 rebuilds the list of active instances.  Waits are bounded: a barrier
+// that does not fill within kPersistSpin polls sets the error word and every
+// CTA returns.
+// ---------------------------------------------------------------------------
+constexpr int kPersistThreads = 256;
+constexpr int kPersistSpin = 1 << 25;   // polls of 64 ns and more per barrier: > 2 s
+
+// The control record (opyx_rof_persist_ctl): barrier arrivals (monotone),
+// work counters of the grabbing phases (mod 4), the error word, the active
+// instances and their strips, the iterations at the last check.
+using PersistCtl = opyx_rof_persist_ctl;
+static_assert(sizeof(opyx_rof_persist_ctl) == 40, "control record layout");
+
+static size_t persist_act_off(int ninst) { return 256 + ((4 * (size_t)ninst + 255) & ~(size_t)255); }
+static size_t persist_part_off(int ninst) {
+  return persist_act_off(ninst) + ((4 * ((size_t)ninst + 1) + 255) & ~(size_t)255);
+}
+
+OPYX_D unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Bounded grid barrier: returns false (every thread of the CTA alike) if it
+// timed out or another CTA reported an error.
+OPYX_D bool grid_sync(PersistCtl* ctl, unsigned long long& nbar) {
+  __shared__ int ok_s;
+  __syncthreads();
+  ++nbar;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd((unsigned long long*)&ctl->arrive, 1ull);
+    const unsigned long long target = nbar * gridDim.x;
+    int ok = 1;
+    for (int i = 0;; ++i) {
+      if (ld_acquire_u64((const unsigned long long*)&ctl->arrive) >= target) break;
+      if (*(volatile int*)&ctl->error || i >= kPersistSpin) {
+        atomicExch(&ctl->error, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// The next work item of a grabbing phase for this warp (the same for all its
+// lanes), or -1 when the phase's nwork items are taken.
+OPYX_D int grab_item(PersistCtl* ctl, unsigned ph, int nwork) {
+  int w = 0;
+  if ((threadIdx.x & 31) == 0) w = (int)atomicAdd((unsigned*)&ctl->grab[ph & 3u], 1u);
+  w = __shfl_sync(0xffffffffu, w, 0);
+  return w < nwork ? w : -1;
+}
+
+// Active instance j holding work item w (act_off ascending, binary search).
+OPYX_D int item_owner(const int* act_off, int nact, int w) {
+  int lo = 0, hi = nact - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldcg(act_off + mid) <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Partial gap sums of one strip (rows [r0, r1), 128 pixels from q_beg) by
+// one warp, with the per-pixel terms of k_gap_batch: {G, |Ax|, G*, |y|^2,
+// max(|y| - lbd)}; each lane sums its quad of a row in FP32 and adds that
+// into FP64 (the objectives are large sums whose difference is the gap),
+// FP64 across the warp in a fixed order.
+OPYX_D void gap_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
+                       int64_t r1, double* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t q0 = q_beg + 4 * lane;
+  const bool act = q0 < g.nl;
+  const int64_t nl = g.nl, nrow = g.n[0];
+  const bool has_r = q0 + 4 < nl, has_l = q0 > 0;
+  double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0;
+  float pinf = -INFINITY;
+  if (act) {
+    float qx[4], qn[4], qf[4], qy[8], qu[8], xr = 0.f, yl = 0.f;
+    auto ld4 = [](float* d, const float* s) {
+      const float4 v = __ldcg(reinterpret_cast<const float4*>(s));
+      d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+    };
+    ld4(qx, a.x + r0 * nl + q0);
+    if (r0 > 0) { ld4(qu, a.y + ((r0 - 1) * nl + q0) * 2); ld4(qu + 4, a.y + ((r0 - 1) * nl + q0) * 2 + 4); }
+    else { for (int j = 0; j < 8; ++j) qu[j] = 0.f; }
+    for (int64_t r = r0; r < r1; ++r) {
+      const int64_t i0 = r * nl + q0;
+      const bool has_up = r > 0, has_dn = r < nrow - 1;
+      if (has_dn) ld4(qn, a.x + i0 + nl);
+      else { for (int j = 0; j < 4; ++j) qn[j] = 0.f; }
+      ld4(qy, a.y + i0 * 2);
+      ld4(qy + 4, a.y + i0 * 2 + 4);
+      {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(a.f + i0));
+        qf[0] = v.x; qf[1] = v.y; qf[2] = v.z; qf[3] = v.w;
+      }
+      xr = has_r ? __ldcg(a.x + i0 + 4) : 0.f;
+      yl = has_l ? __ldcg(a.y + (i0 - 1) * 2 + 1) : 0.f;
+      unsigned mk = 0xffffffffu;
+      if (a.mask) mk = __ldg(reinterpret_cast<const unsigned*>(a.mask + i0));
+      float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f;
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int64_t q = q0 + p;
+        const bool on = (mk >> (8 * p)) & 0xffu;
+        const bool inx = q < nl - 1;
+        float n2 = 0.f, y2 = 0.f;
+        const float xk = qx[p], fk = qf[p];
+        float s = 0.f;
+        const float ihl = g.invh[1], ihr = g.invh[0];
+        if (inx) s -= qy[p * 2 + 1] * ihl;
+        if (q > 0) s += (p > 0 ? qy[(p - 1) * 2 + 1] : yl) * ihl;
+        if (has_dn) s -= qy[p * 2] * ihr;
+        if (has_up) s += qu[p * 2] * ihr;
+        const float ak = g.w[0] * s;
+        if (on) {
+          const float d = xk - fk;
+          pG += g.vol[0] * d * d;
+          pGs += ak * ak * g.half_rvol[0] - fk * ak;
+        }
+        const float nb = p < 3 ? qx[p + 1] : xr;
+        const float gl = inx ? g.coef[1][0] * (nb - xk) : 0.f;
+        const float gr = has_dn ? g.coef[0][0] * (qn[p] - xk) : 0.f;
+        n2 += gl * gl + gr * gr;
+        y2 += qy[p * 2] * qy[p * 2];
+        y2 += qy[p * 2 + 1] * qy[p * 2 + 1];
+        const float nrm = sqrtf(n2);
+        pF += g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
+        pFs += y2;
+        pinf = fmaxf(pinf, sqrtf(y2) - g.lbd);
+      }
+      sG += 0.5 * (double)pG;
+      sF += (double)pF;
+      sGs += (double)pGs;
+      sFs += (double)pFs;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) qx[j] = qn[j];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) qu[j] = qy[j];
+    }
+  }
+  double v[5] = {sG, sF, sGs, sFs, (double)pinf};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double r = warp_reduce(k == 4 ? RED_MAX : RED_SUM, v[k]);
+    if (lane == 0) out[k] = r;
+  }
+}
+
+// CTA-wide fold of instance b's strip partials (fixed order) and its info
+// record with the stop test.
+OPYX_D void fold_inst(const BatchInst& b, const double* partials) {
+  __shared__ double red[5][kPersistThreads / 32];
+  const int n = b.w_ntx * b.w_nty;
+  double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int it = (int)threadIdx.x; it < n; it += blockDim.x)
+    for (int k = 0; k < 5; ++k) {
+      const double v = __ldcg(partials + (size_t)(b.w_beg + it) * 5 + k);
+      tot[k] = k == 4 ? fmax(tot[k], v) : tot[k] + v;
+    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double r = warp_reduce(k == 4 ? RED_MAX : RED_SUM, tot[k]);
+    if (lane == 0) red[k][warp] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[5];
+    for (int k = 0; k < 5; ++k) {
+      t[k] = red[k][0];
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        t[k] = k == 4 ? fmax(t[k], red[k][w]) : t[k] + red[k][w];
+    }
+    write_info(b.g, b.a, t, b.ssd_shift);
+  }
+  __syncthreads();
+}
+
+// CTA 0, thread 0: the instances whose info record is not done, their
+// strips' offsets, and the counts.
+OPYX_D void rebuild_active(const BatchInst* insts, int ninst, PersistCtl* ctl, int* act_inst,
+                           int* act_off, int iters) {
+  if (threadIdx.x != 0) return;
+  int n = 0, off = 0;
+  for (int i = 0; i < ninst; ++i) {
+    if (*(volatile double*)&insts[i].a.info->done != 0.0) continue;
+    act_inst[n] = i;
+    act_off[n] = off;
+    off += insts[i].w_ntx * insts[i].w_nty;
+    ++n;
+  }
+  act_off[n] = off;
+  ctl->nact = n;
+  ctl->nwork = off;
+  ctl->iters = iters;
+}
+
+template <bool PRE>
+__global__ void __launch_bounds__(kPersistThreads, 2)
+k_batch_persist(const BatchInst* __restrict__ insts, int ninst, int R, PersistCtl* ctl,
+                int* act_inst, int* act_off, double* partials, int gran, int maxiter) {
+  unsigned long long nbar = 0;
+  unsigned ph = 0;
+  if (blockIdx.x == 0) rebuild_active(insts, ninst, ctl, act_inst, act_off, 0);
+  if (!grid_sync(ctl, nbar)) return;
+  for (int k = 0; k < maxiter; ++k) {
+    const int nwork = __ldcg(&ctl->nwork), nact = __ldcg(&ctl->nact);
+    if (nwork == 0) break;
+    // ---- iteration k of every active instance
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->grab[(ph + 2) & 3u] = 0u;
+    for (int w = grab_item(ctl, ph, nwork); w >= 0; w = grab_item(ctl, ph, nwork)) {
+      const int j = item_owner(act_off, nact, w);
+      const BatchInst& b = insts[__ldcg(act_inst + j)];
+      const int loc = w - __ldcg(act_off + j);
+      const int tx = loc % b.w_ntx, ty = loc / b.w_ntx;
+      const int64_t r0 = (int64_t)ty * R;
+      const int64_t r1 = r0 + R < b.g.rows ? r0 + R : b.g.rows;
+      const Args<float> a = (k & 1) ? swapped(b.a) : b.a;
+      sweep_strip1<PRE>(b.g, a, (int64_t)tx * 128, r0, r1);
+    }
+    ++ph;
+    if (!grid_sync(ctl, nbar)) return;
+    if ((k + 1) % gran != 0) continue;
+    // ---- gap check after iteration k (an even count: the iterate is in x, y)
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->grab[(ph + 2) & 3u] = 0u;
+    for (int w = grab_item(ctl, ph, nwork); w >= 0; w = grab_item(ctl, ph, nwork)) {
+      const int j = item_owner(act_off, nact, w);
+      const BatchInst& b = insts[__ldcg(act_inst + j)];
+      const int loc = w - __ldcg(act_off + j);
+      const int tx = loc % b.w_ntx, ty = loc / b.w_ntx;
+      const int64_t r0 = (int64_t)ty * R;
+      const int64_t r1 = r0 + R < b.g.rows ? r0 + R : b.g.rows;
+      gap_strip1(b.g, b.a, (int64_t)tx * 128, r0, r1, partials + (size_t)(b.w_beg + loc) * 5);
+    }
+    ++ph;
+    if (!grid_sync(ctl, nbar)) return;
+    for (int j = blockIdx.x; j < nact; j += gridDim.x) fold_inst(insts[__ldcg(act_inst + j)], partials);
+    if (!grid_sync(ctl, nbar)) return;
+    if (blockIdx.x == 0) rebuild_active(insts, ninst, ctl, act_inst, act_off, k + 1);
+    if (!grid_sync(ctl, nbar)) return;
+  }
+}
+
 static int batch_check(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
   int st = validate(p, b);
   if (st) return st;
@@ -1016,6 +1283,8 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
   h->ninst = ninst;
   h->nitems = (int)nitems;
   h->nchannels = C;
+  h->rows_per_item = rows_per_item;
+  h->witems = 0;
   h->pad = 0;
   BatchInst* insts = (BatchInst*)(base + batch_inst_off());
   BatchItem* items = (BatchItem*)(base + batch_item_off(ninst));
@@ -1035,7 +1304,17 @@ int opyx_rof_batch_describe(const opyx_rof_problem* probs, const opyx_rof_buffer
     host_state(p, &bi.st0);
     bi.ssd_shift = p->ssd_shift;
     bi.item_beg = bi.item_end = 0;
+    bi.w_ntx = (int32_t)((p->dims[1] + kStripW - 1) / kStripW);
+    bi.w_nty = (int32_t)((p->dims[0] + rows_per_item - 1) / rows_per_item);
   }
+  // strips of the persistent solve: every instance, active or not
+  int64_t w = 0;
+  for (int i = 0; i < ninst; ++i) {
+    insts[i].w_beg = (int32_t)w;
+    w += (int64_t)insts[i].w_ntx * insts[i].w_nty;
+  }
+  if (w > INT32_MAX) return OPYX_ERR_UNSUPPORTED;
+  h->witems = (int32_t)w;
   // items grouped by tile class; an image's items are consecutive
   int32_t k = 0;
   for (int c = 0; c < kBatchClasses; ++c) {
@@ -1118,6 +1397,49 @@ int opyx_rof_batch_iterate_class(const void* host_desc, const void* dev_desc, in
     if (st) return st;
   }
   return OPYX_OK;
+}
+
+size_t opyx_rof_batch_persist_ws_bytes(const void* host_desc) {
+  if (!host_desc) return 0;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1 || h.witems < 0) return 0;
+  return persist_part_off(h.ninst) + (size_t)h.witems * 5 * sizeof(double);
+}
+
+int opyx_rof_batch_persist(const void* host_desc, const void* dev_desc, void* ws, int gran,
+                           int maxiter, void* stream) {
+  if (!host_desc || !dev_desc || !ws || gran < 2 || (gran & 1) || maxiter < 0 || (maxiter & 1))
+    return OPYX_ERR_ARG;
+  if (((uintptr_t)ws) & 255) return OPYX_ERR_WORKSPACE;
+  const BatchHeader& h = *(const BatchHeader*)host_desc;
+  if (h.ninst < 1 || h.witems < 0 || h.rows_per_item < 1) return OPYX_ERR_ARG;
+  if (h.nchannels != 1) return OPYX_ERR_UNSUPPORTED;
+  const BatchInst* hinst = (const BatchInst*)((const char*)host_desc + batch_inst_off());
+  const int steps = hinst[0].g.steps;
+  for (int i = 1; i < h.ninst; ++i)
+    if (hinst[i].g.steps != steps) return OPYX_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(ws, 0, persist_part_off(h.ninst), s) != cudaSuccess) return OPYX_ERR_LAUNCH;
+  if (maxiter == 0 || h.witems == 0) return OPYX_OK;
+  const BatchInst* insts = (const BatchInst*)((const char*)dev_desc + batch_inst_off());
+  PersistCtl* ctl = (PersistCtl*)ws;
+  int* act_inst = (int*)((char*)ws + 256);
+  int* act_off = (int*)((char*)ws + persist_act_off(h.ninst));
+  double* partials = (double*)((char*)ws + persist_part_off(h.ninst));
+  int ninst = h.ninst, R = h.rows_per_item;
+  void* args[] = {(void*)&insts, &ninst, &R, &ctl, &act_inst, &act_off, &partials, &gran, &maxiter};
+  const bool pre = steps == OPYX_STEPS_PRECOND;
+  const void* fn = pre ? (const void*)k_batch_persist<true> : (const void*)k_batch_persist<false>;
+  static int per_sm[2] = {-1, -1};
+  int& ps = per_sm[pre ? 1 : 0];
+  if (ps < 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, fn, kPersistThreads, 0) !=
+                    cudaSuccess)
+    return OPYX_ERR_LAUNCH;
+  if (ps < 1) return OPYX_ERR_LAUNCH;
+  const unsigned grid = (unsigned)(ps * sm_count());
+  if (cudaLaunchCooperativeKernel(fn, grid, kPersistThreads, args, 0, s) != cudaSuccess)
+    return OPYX_ERR_LAUNCH;
+  return check_launch();
 }
 
 int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* partials,

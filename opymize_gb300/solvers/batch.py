@@ -35,7 +35,8 @@ class BatchROF(object):
     GRAN_RANGE = (10, 100)
     GRAN_PRIOR_ITERS = 1000   # iterations an instance is assumed to need when tuning the interval
 
-    def __init__(self, images, lbd, huber=0.0, tol=1e-4, granularity=10, rows_per_item=None):
+    def __init__(self, images, lbd, huber=0.0, tol=1e-4, granularity=10, rows_per_item=None,
+                 persistent=None):
         if not images:
             raise ValueError("empty batch")
         self.n = len(images)
@@ -47,6 +48,7 @@ class BatchROF(object):
         self.gran = g + (g & 1)   # iterations run in pairs
         self.rows_per_item = rows_per_item
         self.class_streams = True    # width classes on separate streams inside the graphs
+        self._persistent_req = persistent
         lib = _lib.load()
         self.problems = (_lib.opyx_rof_problem * self.n)()
         self.buffers = (_lib.opyx_rof_buffers * self.n)()
@@ -81,6 +83,11 @@ class BatchROF(object):
             self.arrays.append(arr)
             self.dims.append((H, W, C))
         self.C = C
+        # one channel: the whole solve in one persistent launch (else chains
+        # of per-iteration launches captured in graphs)
+        self.persistent = (C == 1) if persistent is None else bool(persistent)
+        if self.persistent and C != 1:
+            raise ValueError("the persistent batched solve takes one-channel images")
         self.rec_bytes = lib.opyx_rof_batch_record_bytes()
         self.records = DeviceArray.zeros((self.n * self.rec_bytes // 8,), np.float64)
         self.launches = 0
@@ -142,6 +149,92 @@ class BatchROF(object):
         _lib.call("opyx_rof_batch_init", desc[0].ctypes.data, desc[1].data_ptr(), stream_ptr())
         self.launches += 1
 
+    # ------------------------------------------------- persistent solve
+    def _persist(self, desc, gran, maxiter):
+        """One cooperative launch: `maxiter` (even) iterations of every active
+        image with a gap check every `gran` (even) iterations, images retiring
+        on the device; returns the control record (error, active, strips,
+        iterations at the last check) once the launch has finished."""
+        lib = _lib.load()
+        wsb = lib.opyx_rof_batch_persist_ws_bytes(desc[0].ctypes.data)
+        if getattr(self, "_pws", None) is None or self._pws.size * 8 < wsb:
+            self._pws = DeviceArray.zeros(((wsb + 7) // 8,), np.float64)
+        _lib.call("opyx_rof_batch_persist", desc[0].ctypes.data, desc[1].data_ptr(),
+                  self._pws.ptr, int(gran), int(maxiter), stream_ptr())
+        self.launches += 2            # the control block's memset and the solve
+        ctl = self._pws.t[:5].cpu().numpy().view(np.int32)
+        # (arrive: u64, grab[4]: u32, error, nact, nwork, iters: i32)
+        error, nact, nwork, iters = (int(v) for v in ctl[6:10])
+        if error:
+            raise _lib.OpyxError("opyx_rof_batch_persist", _lib.OPYX_ERR_LAUNCH,
+                                 "a grid barrier of the persistent solve timed out")
+        return {"active": nact, "strips": nwork, "iters": iters}
+
+    def _autotune_persistent(self, iters):
+        t = torch()
+        best = None
+        active = np.ones(self.n, np.uint8)
+        big = 1 << 30                 # no gap check within the timed iterations
+        for rows in self.ROWS_CANDIDATES:
+            desc, _, _ = self._describe(active, rows)
+            self._init(desc)
+            self._persist(desc, big, 2)   # warm
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            e0.record()
+            self._persist(desc, big, iters)
+            e1.record()
+            t.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best is None or ms < best[0]:
+                best = (ms, rows, desc)
+        self.rows_per_item = best[1]
+        t_it = best[0] / iters
+        self.tuning = {"rows_per_item": best[1], "ms_per_iteration": t_it}
+        if self.gran_auto:
+            desc = best[2]
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            self._init(desc)
+            e0.record()
+            self._persist(desc, 2, 2)      # two iterations and one gap check
+            e1.record()
+            t.cuda.synchronize()
+            t_gap = max(e0.elapsed_time(e1) - 2 * t_it, 1e-3)
+            g = self.check_interval(t_gap, t_it)
+            self.gran = g
+            self.tuning.update(ms_per_gap=t_gap, granularity=g)
+        self._reset()
+        return best[1]
+
+    def _solve_persistent(self, maxiter):
+        active = np.ones(self.n, np.uint8)
+        desc, _, _ = self._describe(active, self.rows_per_item)
+        self._init(desc)
+        t = torch()
+        t0 = time.perf_counter()
+        m = maxiter + (maxiter & 1)
+        self.persist_ctl = self._persist(desc, self.gran, m)
+        t.cuda.synchronize()
+        self.elapsed = time.perf_counter() - t0
+        return self._read_info(maxiter)
+
+    def _read_info(self, maxiter):
+        names = _lib.ROF_INFO_FIELDS
+        nrec = self.rec_bytes // 8
+        i_done, i_fault = names.index("done"), names.index("fault")
+        i_checks = names.index("checks")
+        off = 256 // 8
+        final = self.records.get().reshape(self.n, nrec)[:, off:off + len(names)]
+        if (final[:, i_fault] != 0).any():
+            raise _lib.OpyxError("batched PDHG iteration", _lib.OPYX_ERR_LAUNCH,
+                                 "a kernel gave up waiting for its own copies")
+        self.info = []
+        for i in range(self.n):
+            d = {k: float(final[i, names.index(k)]) for k in INFO_KEYS}
+            d["iter"] = int(min(maxiter, round(final[i, i_checks]) * self.gran))
+            d["converged"] = bool(final[i, i_done] != 0)
+            self.info.append(d)
+        return self.info
+
     def autotune(self, iters=4):
         """Rows per work item: each candidate runs `iters` iterations from the
         zero start, timed with CUDA events; the fastest is kept and the state
@@ -150,6 +243,8 @@ class BatchROF(object):
         and an instance runs on average g/2 iterations past its stop, so g
         minimises t_gap/g + t_iter g/(2 n) for n = GRAN_PRIOR_ITERS, i.e.
         g = sqrt(2 n t_gap / t_iter), even, within GRAN_RANGE."""
+        if self.persistent:
+            return self._autotune_persistent(iters)
         t = torch()
         best = None
         active = np.ones(self.n, np.uint8)
@@ -245,6 +340,8 @@ class BatchROF(object):
                     src = v if hasattr(v, "data_ptr") else t.from_numpy(
                         np.ascontiguousarray(v, dtype=np.float32))
                     arr[key].t.copy_(src.reshape(-1))
+        if self.persistent:
+            return self._solve_persistent(maxiter)
         t = torch()
         names = _lib.ROF_INFO_FIELDS
         nrec = self.rec_bytes // 8

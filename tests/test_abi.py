@@ -188,6 +188,9 @@ ERROR_CASES = [
     ("opyx_rof_iterate_noalloc", (_rof((4096, 4096)), _P, _P, _P, None, 1, None, None),
      _lib.OPYX_ERR_SCRATCH_LIMIT),                                     # xbar does not fit
     ("opyx_rof_iterate_noalloc", (_rof((0, 4)), _P, _P, _P, None, 1, None, None), ARG),
+    ("opyx_rof_batch_persist", (None, None, None, 10, 100, None), ARG),
+    ("opyx_rof_batch_persist", (_P, _P, _P, 7, 100, None), ARG),     # odd check interval
+    ("opyx_rof_batch_persist", (_P, _P, _P, 10, 99, None), ARG),     # odd iteration count
 ]
 
 
