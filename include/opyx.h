@@ -497,14 +497,17 @@ int opyx_rof_batch_gap(const void* host_desc, const void* dev_desc, double* part
  * opyx_rof_batch_persist_ws_bytes(host_desc) bytes, 256-byte aligned; it
  * starts with the control record opyx_rof_persist_ctl (cleared by the call;
  * after the launch `error` != 0 means a barrier timed out -- every wait is
- * bounded -- `nact`/`nwork` are the instances / strips still active and
- * `iters` the iterations at the last check).  Call opyx_rof_batch_init
+ * bounded -- `nact`/`nwork` are the instances / sweep items still active and
+ * `iters` the iterations at the last check).  When few instances remain the
+ * sweep items get fewer rows (rows_per_item halved down to 2) so that every
+ * warp keeps several; the gap uses strips of rows_per_item rows.  Call opyx_rof_batch_init
  * first.  The info records hold each instance's objectives, check count
  * and stop flag as for opyx_rof_batch_gap. */
 typedef struct {
   uint64_t arrive;
   uint32_t grab[4];
   int32_t error, nact, nwork, iters;
+  int32_t rows, nwork_gap;    /* rows of the current sweep items; gap strips */
 } opyx_rof_persist_ctl;
 size_t opyx_rof_batch_persist_ws_bytes(const void* host_desc);
 int opyx_rof_batch_persist(const void* host_desc, const void* dev_desc, void* ws, int gran,

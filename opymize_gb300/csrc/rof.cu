@@ -953,11 +953,18 @@ constexpr int kPersistSpin = 1 << 25;   // polls of 64 ns and more per barrier: 
 // work counters of the grabbing phases (mod 4), the error word, the active
 // instances and their strips, the iterations at the last check.
 using PersistCtl = opyx_rof_persist_ctl;
-static_assert(sizeof(opyx_rof_persist_ctl) == 40, "control record layout");
+static_assert(sizeof(opyx_rof_persist_ctl) == 48, "control record layout");
 
-static size_t persist_act_off(int ninst) { return 256 + ((4 * (size_t)ninst + 255) & ~(size_t)255); }
+// Workspace: the control record, then act_inst (ninst), act_off and
+// act_goff (ninst + 1 each: sweep-item and gap-strip offsets of the active
+// instances), then the strips' gap partials.
+static size_t persist_align(size_t n) { return (n + 255) & ~(size_t)255; }
+static size_t persist_act_off(int ninst) { return 256 + persist_align(4 * (size_t)ninst); }
+static size_t persist_act_goff(int ninst) {
+  return persist_act_off(ninst) + persist_align(4 * ((size_t)ninst + 1));
+}
 static size_t persist_part_off(int ninst) {
-  return persist_act_off(ninst) + ((4 * ((size_t)ninst + 1) + 255) & ~(size_t)255);
+  return persist_act_goff(ninst) + persist_align(4 * ((size_t)ninst + 1));
 }
 
 OPYX_D unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -1130,35 +1137,64 @@ OPYX_D void fold_inst(const BatchInst& b, const double* partials) {
   __syncthreads();
 }
 
-// CTA 0, thread 0: the instances whose info record is not done, their
-// strips' offsets, and the counts.
-OPYX_D void rebuild_active(const BatchInst* insts, int ninst, PersistCtl* ctl, int* act_inst,
-                           int* act_off, int iters) {
+// CTA 0, thread 0: the instances whose info record is not done, the rows
+// of the sweep items (R halved, down to 2, until there are at least
+// kPersistItemsPerWarp items per warp), their sweep-item and gap-strip
+// offsets, and the counts.
+#ifndef OPYX_PERSIST_ITEMS_PER_WARP
+#define OPYX_PERSIST_ITEMS_PER_WARP 4
+#endif
+constexpr int kPersistItemsPerWarp = OPYX_PERSIST_ITEMS_PER_WARP;
+
+OPYX_D void rebuild_active(const BatchInst* insts, int ninst, int R, PersistCtl* ctl, int* act_inst,
+                           int* act_off, int* act_goff, int iters) {
   if (threadIdx.x != 0) return;
-  int n = 0, off = 0;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  int n = 0, goff = 0;
   for (int i = 0; i < ninst; ++i) {
     if (*(volatile double*)&insts[i].a.info->done != 0.0) continue;
     act_inst[n] = i;
-    act_off[n] = off;
-    off += insts[i].w_ntx * insts[i].w_nty;
+    act_goff[n] = goff;
+    goff += insts[i].w_ntx * insts[i].w_nty;
     ++n;
+  }
+  act_goff[n] = goff;
+  int re = R;
+  for (;;) {
+    int64_t items = 0;
+    for (int j = 0; j < n; ++j) {
+      const BatchInst& b = insts[act_inst[j]];
+      items += (int64_t)b.w_ntx * ((b.g.rows + re - 1) / re);
+    }
+    if (re <= 2 || items >= kPersistItemsPerWarp * warps) break;
+    re = (re + 1) / 2;
+  }
+  int off = 0;
+  for (int j = 0; j < n; ++j) {
+    const BatchInst& b = insts[act_inst[j]];
+    act_off[j] = off;
+    off += b.w_ntx * (int)((b.g.rows + re - 1) / re);
   }
   act_off[n] = off;
   ctl->nact = n;
   ctl->nwork = off;
+  ctl->nwork_gap = goff;
+  ctl->rows = re;
   ctl->iters = iters;
 }
 
-template <bool PRE>
+template <bool PRE, bool MASK>
 __global__ void __launch_bounds__(kPersistThreads, 2)
 k_batch_persist(const BatchInst* __restrict__ insts, int ninst, int R, PersistCtl* ctl,
-                int* act_inst, int* act_off, double* partials, int gran, int maxiter) {
+                int* act_inst, int* act_off, int* act_goff, double* partials, int gran,
+                int maxiter) {
   unsigned long long nbar = 0;
   unsigned ph = 0;
-  if (blockIdx.x == 0) rebuild_active(insts, ninst, ctl, act_inst, act_off, 0);
+  if (blockIdx.x == 0) rebuild_active(insts, ninst, R, ctl, act_inst, act_off, act_goff, 0);
   if (!grid_sync(ctl, nbar)) return;
   for (int k = 0; k < maxiter; ++k) {
     const int nwork = __ldcg(&ctl->nwork), nact = __ldcg(&ctl->nact);
+    const int re = __ldcg(&ctl->rows);
     if (nwork == 0) break;
     // ---- iteration k of every active instance
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->grab[(ph + 2) & 3u] = 0u;
@@ -1167,30 +1203,31 @@ k_batch_persist(const BatchInst* __restrict__ insts, int ninst, int R, PersistCt
       const BatchInst& b = insts[__ldcg(act_inst + j)];
       const int loc = w - __ldcg(act_off + j);
       const int tx = loc % b.w_ntx, ty = loc / b.w_ntx;
-      const int64_t r0 = (int64_t)ty * R;
-      const int64_t r1 = r0 + R < b.g.rows ? r0 + R : b.g.rows;
+      const int64_t r0 = (int64_t)ty * re;
+      const int64_t r1 = r0 + re < b.g.rows ? r0 + re : b.g.rows;
       const Args<float> a = (k & 1) ? swapped(b.a) : b.a;
-      sweep_strip1<PRE>(b.g, a, (int64_t)tx * 128, r0, r1);
+      sweep_strip1<PRE, MASK>(b.g, a, (int64_t)tx * kStripW, r0, r1);
     }
     ++ph;
     if (!grid_sync(ctl, nbar)) return;
     if ((k + 1) % gran != 0) continue;
     // ---- gap check after iteration k (an even count: the iterate is in x, y)
+    const int ngap = __ldcg(&ctl->nwork_gap);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->grab[(ph + 2) & 3u] = 0u;
-    for (int w = grab_item(ctl, ph, nwork); w >= 0; w = grab_item(ctl, ph, nwork)) {
-      const int j = item_owner(act_off, nact, w);
+    for (int w = grab_item(ctl, ph, ngap); w >= 0; w = grab_item(ctl, ph, ngap)) {
+      const int j = item_owner(act_goff, nact, w);
       const BatchInst& b = insts[__ldcg(act_inst + j)];
-      const int loc = w - __ldcg(act_off + j);
+      const int loc = w - __ldcg(act_goff + j);
       const int tx = loc % b.w_ntx, ty = loc / b.w_ntx;
       const int64_t r0 = (int64_t)ty * R;
       const int64_t r1 = r0 + R < b.g.rows ? r0 + R : b.g.rows;
-      gap_strip1(b.g, b.a, (int64_t)tx * 128, r0, r1, partials + (size_t)(b.w_beg + loc) * 5);
+      gap_strip1(b.g, b.a, (int64_t)tx * kStripW, r0, r1, partials + (size_t)(b.w_beg + loc) * 5);
     }
     ++ph;
     if (!grid_sync(ctl, nbar)) return;
     for (int j = blockIdx.x; j < nact; j += gridDim.x) fold_inst(insts[__ldcg(act_inst + j)], partials);
     if (!grid_sync(ctl, nbar)) return;
-    if (blockIdx.x == 0) rebuild_active(insts, ninst, ctl, act_inst, act_off, k + 1);
+    if (blockIdx.x == 0) rebuild_active(insts, ninst, R, ctl, act_inst, act_off, act_goff, k + 1);
     if (!grid_sync(ctl, nbar)) return;
   }
 }
@@ -1425,13 +1462,20 @@ int opyx_rof_batch_persist(const void* host_desc, const void* dev_desc, void* ws
   PersistCtl* ctl = (PersistCtl*)ws;
   int* act_inst = (int*)((char*)ws + 256);
   int* act_off = (int*)((char*)ws + persist_act_off(h.ninst));
+  int* act_goff = (int*)((char*)ws + persist_act_goff(h.ninst));
   double* partials = (double*)((char*)ws + persist_part_off(h.ninst));
   int ninst = h.ninst, R = h.rows_per_item;
-  void* args[] = {(void*)&insts, &ninst, &R, &ctl, &act_inst, &act_off, &partials, &gran, &maxiter};
+  void* args[] = {(void*)&insts, &ninst, &R, &ctl, &act_inst, &act_off, &act_goff, &partials,
+                  &gran, &maxiter};
+  bool mask = false;
+  for (int i = 0; i < h.ninst; ++i) mask |= hinst[i].a.mask != nullptr;
   const bool pre = steps == OPYX_STEPS_PRECOND;
-  const void* fn = pre ? (const void*)k_batch_persist<true> : (const void*)k_batch_persist<false>;
-  static int per_sm[2] = {-1, -1};
-  int& ps = per_sm[pre ? 1 : 0];
+  const void* fn = pre ? (mask ? (const void*)k_batch_persist<true, true>
+                               : (const void*)k_batch_persist<true, false>)
+                       : (mask ? (const void*)k_batch_persist<false, true>
+                               : (const void*)k_batch_persist<false, false>);
+  static int per_sm[4] = {-1, -1, -1, -1};
+  int& ps = per_sm[(pre ? 2 : 0) + (mask ? 1 : 0)];
   if (ps < 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, fn, kPersistThreads, 0) !=
                     cudaSuccess)
     return OPYX_ERR_LAUNCH;

@@ -140,6 +140,7 @@ OPYX_D void stg4(float* p, float a0, float a1, float a2, float a3) {
 
 // Row r (none if r is outside [0, rows)) for the lane whose quad starts at
 // q0; act: the quad lies in the image.
+template <bool MASK>
 OPYX_D Row1 load_row1(const Geo<float>& g, const Args<float>& a, int64_t r, int64_t q0, bool act,
                       int lane) {
   Row1 d;
@@ -155,7 +156,7 @@ OPYX_D Row1 load_row1(const Geo<float>& g, const Args<float>& a, int64_t r, int6
     d.y23 = ldcg4(a.y + i0 * 2 + 4);
     d.xv = ldcg4(a.x + i0);
     d.fv = ldg4(a.f + i0);
-    if (a.mask) d.mk = __ldg(reinterpret_cast<const unsigned*>(a.mask + i0));
+    if (MASK) d.mk = __ldg(reinterpret_cast<const unsigned*>(a.mask + i0));
   }
   if (lane == 0 && act && q0 > 0) d.yl = __ldcg(a.y + i0 * 2 - 1);
   if (lane == 31 && q0 + 4 < g.nl) {
@@ -164,15 +165,16 @@ OPYX_D Row1 load_row1(const Geo<float>& g, const Args<float>& a, int64_t r, int6
     d.hy1 = h.y;
     d.hx = __ldcg(a.x + i0 + 4);
     d.hf = __ldg(a.f + i0 + 4);
-    if (a.mask) d.hm = __ldg(a.mask + i0 + 4);
+    if (MASK) d.hm = __ldg(a.mask + i0 + 4);
   }
   return d;
 }
 
 // One iteration on rows [r0, r1) of the strip of 128 pixels starting at
 // q_beg (clipped to the image), by one warp: lane l owns the quad at
-// q_beg + 4 l.  Reads a.x, a.y, a.f; writes a.x2, a.y2.
-template <bool PRE>
+// q_beg + 4 l.  Reads a.x, a.y, a.f; writes a.x2, a.y2.  MASK: a.mask is
+// set (else the SSD term applies everywhere).
+template <bool PRE, bool MASK>
 OPYX_D void sweep_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
                          int64_t r1) {
   const int lane = threadIdx.x & 31;
@@ -188,16 +190,16 @@ OPYX_D void sweep_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_be
   float py0[4], py1[4], pxb[4], phb = 0.f, phy0;
   {
     // y_k of the row above the run (across rows) for pass A of its first row
-    const Row1 u = load_row1(g, a, r0 - 1, q0, act, lane);
+    const Row1 u = load_row1<MASK>(g, a, r0 - 1, q0, act, lane);
     py0[0] = u.y01.x; py0[1] = u.y01.z; py0[2] = u.y23.x; py0[3] = u.y23.z;
     py1[0] = u.y01.y; py1[1] = u.y01.w; py1[2] = u.y23.y; py1[3] = u.y23.w;
     phy0 = u.hy0;
   }
 #pragma unroll
   for (int p = 0; p < 4; ++p) pxb[p] = 0.f;
-  Row1 cur = load_row1(g, a, r0, q0, act, lane);
+  Row1 cur = load_row1<MASK>(g, a, r0, q0, act, lane);
   for (int64_t r = r0; r <= r1; ++r) {
-    const Row1 nxt = load_row1(g, a, r + 1 <= rl ? r + 1 : -1, q0, act, lane);
+    const Row1 nxt = load_row1<MASK>(g, a, r + 1 <= rl ? r + 1 : -1, q0, act, lane);
     const bool has_up = r > 0, has_dn = r < g.rows - 1;
     const float cy0[4] = {cur.y01.x, cur.y01.z, cur.y23.x, cur.y23.z};
     const float cy1[4] = {cur.y01.y, cur.y01.w, cur.y23.y, cur.y23.w};
@@ -212,20 +214,20 @@ OPYX_D void sweep_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_be
       if (qin && has_up && has_dn) {
 #pragma unroll
         for (int p = 0; p < 4; ++p)
-          pass_a1<true>(g, pre, pc, ci, q0 + p, ((cur.mk >> (8 * p)) & 0xffu) != 0, has_up,
+          pass_a1<true>(g, pre, pc, ci, q0 + p, !MASK || ((cur.mk >> (8 * p)) & 0xffu) != 0, has_up,
                         has_dn, cy1[p], p > 0 ? cy1[p - 1] : yl0, cy0[p], py0[p], xo[p], fq[p],
                         xn[p], cxb[p]);
       } else {
 #pragma unroll
         for (int p = 0; p < 4; ++p)
           pass_a1<false>(g, pre, pc, ci, q0 + p,
-                         q0 + p >= g.nl || ((cur.mk >> (8 * p)) & 0xffu) != 0, has_up, has_dn,
+                         !MASK || q0 + p >= g.nl || ((cur.mk >> (8 * p)) & 0xffu) != 0, has_up, has_dn,
                          cy1[p], p > 0 ? cy1[p - 1] : yl0, cy0[p], py0[p], xo[p], fq[p], xn[p],
                          cxb[p]);
       }
       if (lane == 31) {
         float hxn;
-        pass_a1<false>(g, pre, pc, ci, q0 + 4, q0 + 4 >= g.nl || cur.hm != 0, has_up, has_dn,
+        pass_a1<false>(g, pre, pc, ci, q0 + 4, !MASK || q0 + 4 >= g.nl || cur.hm != 0, has_up, has_dn,
                        cur.hy1, cy1[3], cur.hy0, phy0, cur.hx, cur.hf, hxn, chb);
       }
       if (r < r1 && act) stg4(a.x2 + r * g.nl + q0, xn[0], xn[1], xn[2], xn[3]);

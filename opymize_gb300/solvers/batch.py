@@ -162,13 +162,13 @@ class BatchROF(object):
         _lib.call("opyx_rof_batch_persist", desc[0].ctypes.data, desc[1].data_ptr(),
                   self._pws.ptr, int(gran), int(maxiter), stream_ptr())
         self.launches += 2            # the control block's memset and the solve
-        ctl = self._pws.t[:5].cpu().numpy().view(np.int32)
-        # (arrive: u64, grab[4]: u32, error, nact, nwork, iters: i32)
-        error, nact, nwork, iters = (int(v) for v in ctl[6:10])
+        ctl = self._pws.t[:6].cpu().numpy().view(np.int32)
+        # (arrive: u64, grab[4]: u32, error, nact, nwork, iters, rows, nwork_gap: i32)
+        error, nact, nwork, iters, rows = (int(v) for v in ctl[6:11])
         if error:
             raise _lib.OpyxError("opyx_rof_batch_persist", _lib.OPYX_ERR_LAUNCH,
                                  "a grid barrier of the persistent solve timed out")
-        return {"active": nact, "strips": nwork, "iters": iters}
+        return {"active": nact, "items": nwork, "iters": iters, "item_rows": rows}
 
     def _autotune_persistent(self, iters):
         t = torch()
