@@ -197,6 +197,55 @@ int opyx_epigraph_proj(const opyx_epigraph* e, int dtype, const void* x, void* y
 int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void* x,
                        double* out, void* ws, void* stream);
 
+/* ---------------------------------------------- fused sublabel-lifted model */
+/* One fused pass of the PDHG iteration (opymize/solvers/pdhg.py:124-187) of
+ * the sublabel-lifted scalar model that opymize_gb300/tools/lifting.py
+ * assembles from the reference's operators:
+ *   x = (u [N, L], gamma [N], mu [L-1, N, 2]),
+ *   y = (q [N, L], e [N], p [N, 2], s [N], z [L-1, N, 2]),
+ *   A x = (u + IndexedMultAdj(mu) [P[j] = (j, j+1), coefficients B],
+ *          <t, u> - gamma, forward gradient of gamma (h = 1), <1, u>, mu),
+ *   prox_tauG = (max(u, 0), gamma, mu),
+ *   prox_sigmaF* = (q, e, projection of p onto |p_i| <= lbd, s - sigma,
+ *                   EpigraphInd projection of every z[j, i] (ndim 1)).
+ * which = 0 (pass A): xkp1 = prox(xk - tau A^T yk), xbar = (1+theta) xkp1 -
+ * theta xk; which = 1 (pass B): ykp1 = prox(yk + sigma A xbar).  It replaces
+ * the generic path's chain of BlockOp / IndexedMultAdj / MatrixMultR /
+ * ScaleOp / GradientOp and prox launches for this model (about 22 per
+ * iteration).  Steps: tau and sigma of u, mu, q, e, s, z per label /
+ * interval / component (the same for every pixel, as the preconditioner
+ * of this A gives), gamma's tau and p's sigma per pixel (tau_g (N), sig_p
+ * (N, 2) device arrays) or, if NULL, the scalars tau_g0, sig_p0.  The
+ * epigraph data: v (npoints) points, bt (npoints, N) values at the points,
+ * It (npoints, N) point masks or NULL (all set), J (L-1, nsub) the points
+ * of each interval (nsub <= 16).  L: 2 to 32. */
+typedef struct {
+  int32_t dtype, L, nsub, pad;
+  int64_t H, W;
+  const void* xk;
+  void* xkp1;
+  void* xbar;
+  const void* yk;
+  void* ykp1;
+  double t[32];
+  double B[31 * 2 * 2];          /* B[j][m][k] */
+  double tau_u[32], tau_mu[31 * 2];
+  double sig_q[32], sig_z[31 * 2];
+  double sig_e, sig_s;
+  const void* tau_g;
+  const void* sig_p;
+  double tau_g0, sig_p0;
+  double lbd, theta;
+  const void* v;
+  const void* bt;
+  const uint8_t* It;
+  const int64_t* J;
+  int32_t sorted;                /* perm gives each interval's points by increasing, */
+  uint8_t perm[31 * 16];         /* distinct slope (the projection skips its sort)   */
+  double vsorted[31 * 16];       /* those slopes, in that order (host copy)          */
+} opyx_sublabel;
+int opyx_sublabel_pass(const opyx_sublabel* d, int which, void* stream);
+
 /* ------------------------------------------- piecewise convexification (host) */
 /* The lower convex hull of every function's graph over every region, the
  * input data of EpigraphInd / EpigraphSupp (I = base, If = faces):

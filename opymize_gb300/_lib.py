@@ -79,6 +79,20 @@ class opyx_epigraph(C.Structure):
                 ("bt", C.c_void_p), ("It", C.c_void_p)]
 
 
+class opyx_sublabel(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("L", C.c_int32), ("nsub", C.c_int32), ("pad", C.c_int32),
+                ("H", C.c_int64), ("W", C.c_int64), ("xk", C.c_void_p), ("xkp1", C.c_void_p),
+                ("xbar", C.c_void_p), ("yk", C.c_void_p), ("ykp1", C.c_void_p),
+                ("t", C.c_double * 32), ("B", C.c_double * 124), ("tau_u", C.c_double * 32),
+                ("tau_mu", C.c_double * 62), ("sig_q", C.c_double * 32),
+                ("sig_z", C.c_double * 62), ("sig_e", C.c_double), ("sig_s", C.c_double),
+                ("tau_g", C.c_void_p), ("sig_p", C.c_void_p), ("tau_g0", C.c_double),
+                ("sig_p0", C.c_double), ("lbd", C.c_double), ("theta", C.c_double),
+                ("v", C.c_void_p), ("bt", C.c_void_p), ("It", C.c_void_p), ("J", C.c_void_p),
+                ("sorted", C.c_int32), ("perm", C.c_uint8 * (31 * 16)),
+                ("vsorted", C.c_double * (31 * 16))]
+
+
 class opyx_rof_problem(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("ndim", C.c_int32), ("nchannels", C.c_int32),
                 ("steps", C.c_int32), ("dims", C.c_int64 * 3), ("h", C.c_double * 3),
@@ -186,6 +200,7 @@ SIGNATURES = {
     "opyx_rof_batch_gap": (i32, [vp, vp, vp, vp]),
     "opyx_rof_batch_persist_ws_bytes": (sz, [vp]),
     "opyx_rof_batch_persist": (i32, [vp, vp, vp, i32, i32, vp]),
+    "opyx_sublabel_pass": (i32, [P(opyx_sublabel), i32, vp]),
     "opyx_conv3x3": (i32, [P(opyx_conv3x3_desc), vp]),
     "opyx_conv3x3_wgrad_workspace": (sz, [P(opyx_conv3x3_desc)]),
     "opyx_conv3x3_wgrad": (i32, [P(opyx_conv3x3_desc), vp, vp, i32, vp, sz, vp]),

@@ -14,6 +14,7 @@
 // an orthonormal basis of the working set's normals (|W| <= n+1 <= 4), for
 // every n alike (ActiveBasis below).
 #include "common.cuh"
+#include "epi1_dev.cuh"
 
 namespace opyx {
 namespace epi {
@@ -368,24 +369,7 @@ k_proj(opyx_epigraph e, const T* __restrict__ x, T* y, int maxiter, double tol,
 }
 
 // ndim = 1 with at most kDirect constraints per instance: the exact
-// projection in one pass, no iterations.  The constraints bound the
-// epigraph of g(s) = max_l (v_l s - b_l), a convex piecewise-linear function
-// of one variable.  With the lines sorted by slope (then by offset), line k
-// is the graph of g on [lo_k, hi_k],
-//   lo_k = max over m < k of (b_k - b_m) / (v_k - v_m),
-//   hi_k = min over m > k of (b_k - b_m) / (v_k - v_m)
-// (no piece if lo_k > hi_k or an earlier line has the same slope), and the
-// pieces follow each other left to right.  The projection p of a point x
-// below the graph is the point where x - p lies in the normal cone, found by
-// a left-to-right scan with first-order tests only:
-//  * inside piece k:  x violates line k and the orthogonal projection onto
-//    the line, s = (s0 + v_k (t0 + b_k)) / (1 + v_k^2), is in [lo_k, hi_k];
-//  * at the vertex V between pieces L and R:  (V - x).(1, v_L) <= 0 <=
-//    (V - x).(1, v_R) (x - V between the two outward normals).
-// Comparing squared distances instead resolves p only to sqrt(eps) of the
-// distance (in FP32 errors up to 1e-4 on the sublabel model's iterates).
-// If rounding leaves no test true, the nearest candidate is taken.  Points
-// with no positive violation are kept, as by the active-set method.  The
+// projection in one pass, no iterations (project1, epi1_dev.cuh).  The
 // result is the QP's solution up to rounding, so instances never count as
 // not converged.  Optional transposed copies bt (npoints, nfuns) of b and
 // It of I make the reads of neighbouring instances (consecutive i)
@@ -402,11 +386,8 @@ k_proj1(opyx_epigraph e, const T* __restrict__ x, T* y) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = t / e.nfuns, i = t - j * e.nfuns;
-    const T s0 = x[2 * t], t0 = x[2 * t + 1];
     T cv[NS], cb[NS];
     bool on[NS];
-    T viol = T(0);
-    bool any = false;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       const bool used = k < e.nsubpoints;
@@ -414,77 +395,9 @@ k_proj1(opyx_epigraph e, const T* __restrict__ x, T* y) {
       on[k] = used && (e.It ? e.It[l * e.nfuns + i] : e.I[i * e.npoints + l]) != 0;
       cv[k] = on[k] ? v[l] : T(0);
       cb[k] = on[k] ? (bt ? bt[l * e.nfuns + i] : b[i * e.npoints + l]) : T(0);
-      if (on[k]) {
-        const T r = cv[k] * s0 - t0 - cb[k];
-        if (!any || r > viol) viol = r;
-        any = true;
-      }
     }
-    T ys = s0, yt = t0;
-    if (any && viol > T(0)) {
-      // sort by (off last, slope, offset): odd-even transposition, static indices
-#pragma unroll
-      for (int pass = 0; pass < NS; ++pass) {
-#pragma unroll
-        for (int k = pass & 1; k + 1 < NS; k += 2) {
-          const bool sw = (!on[k] && on[k + 1]) ||
-                          (on[k] && on[k + 1] &&
-                           (cv[k + 1] < cv[k] || (cv[k + 1] == cv[k] && cb[k + 1] < cb[k])));
-          if (sw) {
-            const T tv = cv[k], tb = cb[k];
-            const bool to = on[k];
-            cv[k] = cv[k + 1]; cb[k] = cb[k + 1]; on[k] = on[k + 1];
-            cv[k + 1] = tv; cb[k + 1] = tb; on[k + 1] = to;
-          }
-        }
-      }
-      bool found = false, have_prev = false;
-      T pv = T(0);                       // slope of the previous piece
-      T best = T(INFINITY), fs = s0, ft = t0;
-#pragma unroll
-      for (int k = 0; k < NS; ++k) {
-        if (!on[k]) continue;
-        T lo = -T(INFINITY), hi = T(INFINITY);
-        bool live = true;
-#pragma unroll
-        for (int m = 0; m < NS; ++m) {
-          if (m == k || !on[m]) continue;
-          const T dv = cv[k] - cv[m];
-          if (m < k) {
-            if (dv > T(0)) lo = fmax(lo, (cb[k] - cb[m]) / dv);
-            else live = false;           // an earlier line of the same slope lies above
-          } else if (dv < T(0)) {
-            hi = fmin(hi, (cb[k] - cb[m]) / dv);
-          }
-        }
-        if (!live || lo > hi) continue;
-        // the vertex shared with the previous piece
-        if (have_prev && !found) {
-          const T vs = lo, vt = cv[k] * lo - cb[k];
-          const T dl = (vs - s0) + pv * (vt - t0), dr = (vs - s0) + cv[k] * (vt - t0);
-          if (dl <= T(0) && dr >= T(0)) { found = true; ys = vs; yt = vt; }
-          const T d = (vs - s0) * (vs - s0) + (vt - t0) * (vt - t0);
-          if (d < best) { best = d; fs = vs; ft = vt; }
-        }
-        // the inside of piece k
-        if (!found) {
-          const T sk = (s0 + cv[k] * (t0 + cb[k])) / (T(1) + cv[k] * cv[k]);
-          const T r = cv[k] * s0 - t0 - cb[k];
-          if (r > T(0) && sk >= lo && sk <= hi) {
-            found = true;
-            ys = sk;
-            yt = cv[k] * sk - cb[k];
-          } else {
-            const T sc = fmin(fmax(sk, lo), hi), tc = cv[k] * sc - cb[k];
-            const T d = (sc - s0) * (sc - s0) + (tc - t0) * (tc - t0);
-            if (d < best) { best = d; fs = sc; ft = tc; }
-          }
-        }
-        pv = cv[k];
-        have_prev = true;
-      }
-      if (!found) { ys = fs; yt = ft; }
-    }
+    T ys, yt;
+    project1<T, NS>(cv, cb, on, x[2 * t], x[2 * t + 1], ys, yt);
     y[2 * t] = ys;
     y[2 * t + 1] = yt;
   }

@@ -10,7 +10,9 @@ dictionary.  Two device paths:
   104-byte info record once per check;
 * generic -- any composition of GPU operators and functionals: the
   reference's iteration with the step kernels of libopyx, adaptive steps
-  updated on the device, the gap from FP64 device reductions.
+  updated on the device, the gap from FP64 device reductions; the
+  sublabel-lifted model of tools.lifting runs there as two fused passes per
+  iteration (``path == "sublabel"``, solvers/sublabel.py).
 
 ``use_gpu=False`` is refused: this package has no CPU path.
 """
@@ -28,6 +30,7 @@ from opymize_gb300.linear.diff import GradientOp
 from opymize_gb300.functionals.quad import SSD
 from opymize_gb300.functionals.l1norms import L1Norms, HuberL1Norms
 from opymize_gb300.tools import truncate
+from opymize_gb300.solvers.sublabel import SublabelPasses
 from opymize_gb300.tools.util import GracefulInterruptHandler
 
 INFO_KEYS = ("objp", "objd", "infeasp", "infeasd", "gap", "relgap")
@@ -119,7 +122,7 @@ class PDHG(object):
         if use_fused:
             self._solve_fused(*args, graph=graph)
         else:
-            self._solve_generic(*args, graph=graph)
+            self._solve_generic(*args, graph=graph, sublabel=fused is not False)
         return self.info
 
     @property
@@ -256,7 +259,7 @@ class PDHG(object):
 
     # ------------------------------------------------------------ generic
     def _solve_generic(self, dtype, steps, term_pd_gap, term_pd_res, pd_res_mode,
-                       term_maxiter, granularity, cbfun, graph=True):
+                       term_maxiter, granularity, cbfun, graph=True, sublabel=True):
         i, c = self.itervars, self.constvars
         v = {}
         v['xk'], v['yk'] = self._start(dtype)
@@ -288,10 +291,24 @@ class PDHG(object):
         ws = DeviceArray.zeros(((_lib.load().opyx_reduce_workspace_size() + 7) // 8,),
                                np.float64)
         theta = c['theta']
+        # the sublabel-lifted model (tools.lifting) iterates as two fused passes
+        fsub = None
+        if sublabel and st is None and not pd_res_mode:
+            try:
+                fsub = SublabelPasses.make(self, dtype, steps, tau, sigma, theta)
+            except ValueError as err:
+                logging.info("sublabel model stays on the generic path: %s", err)
+        if fsub is not None:
+            self.path = "sublabel"
+        self._sublabel = fsub
 
         def iterate():
             """Launch one iteration (pdhg.py:124-187) and swap the roles of
             the k and k+1 buffers."""
+            if fsub is not None:
+                fsub.iterate(v)
+                swap(1)
+                return
             s = stream_ptr()
             _lib.call("opyx_take_step", v['xk'].dcode, v['xk'].size, v['xkp1'].ptr,
                       v['xk'].ptr, -1, step_struct(tau, dtype), v['xgradk'].ptr, s)
@@ -337,7 +354,7 @@ class PDHG(object):
         def run(n):
             nonlocal parity, capture
             while n > 0:
-                m = min(n, _GENERIC_CHUNK)
+                m = min(n, _SUBLABEL_CHUNK if fsub is not None else _GENERIC_CHUNK)
                 g = graphs.get((m, parity)) if capture else None
                 if g is None and capture:
                     saved = dict(v)
@@ -378,6 +395,11 @@ class PDHG(object):
                         i['tauk'], i['sigmak'], i['alphak'] = h.tau, h.sigma, h.alpha
                         self.info.update(resp=h.resp, resd=h.resd, epsp=h.epsp, epsd=h.epsd)
                     if not pd_res_mode:
+                        if fsub is not None:
+                            # the fused passes keep no A x_k, A^T y_k: the gap's
+                            # operator values come from the generic operators
+                            self.linop(v['xk'], v['ygradk'])
+                            self.linop.adjoint(v['yk'], v['xgradk'])
                         self.info.update(self.pd_gap())
                     el = time.perf_counter() - t0
                     self.info['time_s'], self.info['it_per_s'] = el, _iter / el
@@ -539,6 +561,7 @@ class _FusedLoop(object):
 # iterations per CUDA graph of the generic path (even: a replay keeps the
 # buffer roles)
 _GENERIC_CHUNK = 2
+_SUBLABEL_CHUNK = 16    # two launches per fused sublabel iteration: longer graphs are cheap
 
 
 class _GenericGraph(object):

@@ -123,4 +123,6 @@ def sublabel_problem(f_img, L=16, lbd=0.1, samples=8, trunc=0.04, with_faces=Fal
         [0, GradientOp(dims, 1, scheme="forward"), 0],
         [MatrixMultR(N, np.ones((L, 1))), 0, 0],
         [0, 0, IdentityOp(nmu)]])
+    # the model's data, for PDHG.solve's fused passes (solvers/sublabel.py)
+    A.sublabel = dict(L=L, lbd=lbd, dims=dims, data=d, epi=f.fcts[-1])
     return g, f, A, d

@@ -61,6 +61,7 @@ STRUCTS = {
     "opyx_rof_problem": _lib.opyx_rof_problem,
     "opyx_rof_buffers": _lib.opyx_rof_buffers,
     "opyx_rof_info": _lib.opyx_rof_info,
+    "opyx_sublabel": _lib.opyx_sublabel,
     "opyx_conv3x3_desc": _lib.opyx_conv3x3_desc,
 }
 
