@@ -330,11 +330,14 @@ def gray_case(a, size=2048, lbd=0.1, gran=10, cpu_iters=20):
     return rec
 
 
-def sublabel_case(a, iters=200):
+def sublabel_case(a, iters=5000):
     """The sublabel-lifted configuration: 512^2, 16 labels on [0, 1],
     rho = min((u - f)^2, 0.04) sampled at 8 points per interval, 10%
-    salt-and-pepper, TV weight 0.1, FP32 generic PDHG path with precond
-    steps; iterations per second over `iters` iterations (gap at the end)."""
+    salt-and-pepper, TV weight 0.1, preconditioned steps, `iters`
+    iterations in FP32 (the fused sublabel passes) and the same solve in
+    FP64 (pinned to the reference's CPU solver at 1e-10 on the fixtures):
+    iterations per second, the HBM fraction of the iteration, the gap and
+    infeasibilities of both and the FP32 error against FP64."""
     from opymize_gb300.gpuarray import torch
     from opymize_gb300.solvers import PDHG
     from opymize_gb300.tools import lifting
@@ -342,22 +345,45 @@ def sublabel_case(a, iters=200):
     t = torch()
     img = np.clip(piecewise_constant((512, 512), 1, sigma=0.05, seed=a.seed,
                                      salt_pepper=0.1)[..., 0], 0, 1)
-    g, f, A, _ = lifting.sublabel_problem(img, L=16, lbd=0.1, samples=8)
-    s = PDHG(g, f, A)
-    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=20,
-            granularity=20)
-    t.cuda.synchronize()
-    t0 = time.perf_counter()
-    s.solve(steps="precond", precision="float", term_pd_gap=1e-300, term_maxiter=iters,
-            granularity=iters)
-    t.cuda.synchronize()
-    el = time.perf_counter() - t0
-    return {"workload": "sublabel lifting 512^2, 16 labels, 8 samples/interval, fp32, "
-                        "generic PDHG path, precond steps",
-            "iters_per_s": round(iters / el, 1), "iters": iters,
-            "relgap_after": s.info.get("relgap"),
-            "qp_nonconverged": f.fcts[-1].conj.prox(1.0).nonconverged,
-            "note": "wall time of solve() incl. setup of steps and one final gap"}
+    res = {"workload": "sublabel lifting 512^2, 16 labels, 8 samples/interval, truncated "
+                       "quadratic data term, lambda 0.1, precond steps, %d iterations" % iters}
+    states = {}
+    for precision in ("float", "double"):
+        g, f, A, _ = lifting.sublabel_problem(img, L=16, lbd=0.1, samples=8)
+        s = PDHG(g, f, A)
+        s.solve(steps="precond", precision=precision, term_pd_gap=1e-300, term_maxiter=20,
+                granularity=20)
+        t.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.solve(steps="precond", precision=precision, term_pd_gap=1e-300, term_maxiter=iters,
+                granularity=iters)
+        t.cuda.synchronize()
+        el = time.perf_counter() - t0
+        states[precision] = s.state
+        res[precision] = {"path": s.path, "wall_s": round(el, 3),
+                          "iters_per_s": round(iters / el, 1),
+                          "loop_iters_per_s": round(float(s.info["it_per_s"]), 1),
+                          "relgap": s.info["relgap"], "objp": s.info["objp"],
+                          "objd": s.info["objd"], "infeasp": s.info["infeasp"],
+                          "infeasd": s.info["infeasd"]}
+    (x32, y32), (x64, y64) = states["float"], states["double"]
+    res["fp32_vs_fp64"] = {
+        "x_rel_l2": float(np.linalg.norm(x32 - x64) / np.linalg.norm(x64)),
+        "y_rel_l2": float(np.linalg.norm(y32 - y64) / np.linalg.norm(y64)),
+        "relgap_abs_diff": abs(res["float"]["relgap"] - res["double"]["relgap"])}
+    N, L = 512 * 512, 16
+    n_p, n_d = L + 1 + 2 * (L - 1), 3 * L + 2
+    alg = 4.0 * N * (5 * n_p + 3 * n_d)               # iterates, two-pass count
+    data = 4.0 * N * 8 * (L - 1)                       # the data term at the interval points
+    it_s = res["float"]["loop_iters_per_s"]
+    peak = measured_peaks().get("hbm_gbs")
+    res["hbm"] = {"algorithmic_bytes_per_iter": alg, "data_term_bytes_per_iter": data,
+                  "GBps": round((alg + data) * it_s / 1e9, 1),
+                  "frac_of_measured_hbm": round((alg + data) * it_s / 1e9 / peak, 3)
+                  if peak else None}
+    res["note"] = ("wall time of solve() includes its set-up (steps, initial A x, the fused "
+                   "passes' tables) and the final gap; loop_iters_per_s is the iteration loop")
+    return res
 
 
 def batch_specs(seed, n=512):

@@ -200,17 +200,20 @@ OPYX_D void z_project(const Args<T>& a, int j, int64_t i) {
   z_n[o + 1] = yt;
 }
 
-// ---- pass B: blockIdx.y = 0 the q, e, p, s blocks of every pixel,
-// blockIdx.y = 1 + j the z block of interval j
-template <typename T, int LT, int NS, bool SORTED>
+// ---- pass B, z blocks: blockIdx.y = j the interval (a kernel of its own:
+// far fewer registers than the pixel part, so twice the resident warps for
+// this compute-bound part)
+template <typename T, int NS, bool SORTED>
+__global__ void __launch_bounds__(kThreads, 8) k_pass_z(Args<T> a) {
+  const int j = (int)blockIdx.y;
+  SUB_GRID_STRIDE(i, a.N) z_project<T, NS, SORTED>(a, j, i);
+}
+
+// ---- pass B, the q, e, p, s blocks of every pixel
+template <typename T, int LT>
 __global__ void __launch_bounds__(kThreads, 4) k_pass_b(Args<T> a) {
   const int64_t N = a.N, W = a.W;
   const int L = a.L;
-  if (blockIdx.y > 0) {
-    const int j = (int)blockIdx.y - 1;
-    SUB_GRID_STRIDE(i, N) z_project<T, NS, SORTED>(a, j, i);
-    return;
-  }
   const T* ub = a.xbar;
   const T* gb = a.xbar + N * L;
   const T* mub = a.xbar + N * L + N;
@@ -286,15 +289,18 @@ static int launch_l(const Args<T>& a, int which, cudaStream_t s) {
   const unsigned g = grid_for(a.N, kThreads, 8);
   if (which == 0) {
     k_pass_a<T, LT><<<g, kThreads, 0, s>>>(a);
+    return check_launch();
+  }
+  k_pass_b<T, LT><<<g, kThreads, 0, s>>>(a);
+  int st = check_launch();
+  if (st) return st;
+  const dim3 grid(g, (unsigned)(a.L - 1), 1);   // every interval's z blocks
+  if (a.nsub <= 8) {
+    if (a.sorted) k_pass_z<T, 8, true><<<grid, kThreads, 0, s>>>(a);
+    else k_pass_z<T, 8, false><<<grid, kThreads, 0, s>>>(a);
   } else {
-    const dim3 grid(g, (unsigned)a.L, 1);   // the pixel blocks and L - 1 intervals
-    if (a.nsub <= 8) {
-      if (a.sorted) k_pass_b<T, LT, 8, true><<<grid, kThreads, 0, s>>>(a);
-      else k_pass_b<T, LT, 8, false><<<grid, kThreads, 0, s>>>(a);
-    } else {
-      if (a.sorted) k_pass_b<T, LT, 16, true><<<grid, kThreads, 0, s>>>(a);
-      else k_pass_b<T, LT, 16, false><<<grid, kThreads, 0, s>>>(a);
-    }
+    if (a.sorted) k_pass_z<T, 16, true><<<grid, kThreads, 0, s>>>(a);
+    else k_pass_z<T, 16, false><<<grid, kThreads, 0, s>>>(a);
   }
   return check_launch();
 }
