@@ -83,8 +83,9 @@ class BatchROF(object):
             self.arrays.append(arr)
             self.dims.append((H, W, C))
         self.C = C
-        # one channel: the whole solve in one persistent launch (else chains
-        # of per-iteration launches captured in graphs)
+        # one channel: the whole solve in one persistent launch or chains of
+        # per-iteration launches captured in graphs, whichever the autotuner
+        # times faster (persistent until then); more channels: graphs
         self.persistent = (C == 1) if persistent is None else bool(persistent)
         if self.persistent and C != 1:
             raise ValueError("the persistent batched solve takes one-channel images")
@@ -236,6 +237,31 @@ class BatchROF(object):
         return self.info
 
     def autotune(self, iters=4):
+        """Rows per work item (and the check interval with granularity=None);
+        for one-channel batches whose mode was not fixed by `persistent`,
+        also the mode: the persistent launch and the graph-captured
+        per-iteration launches are both tuned and the faster iteration over
+        the whole batch is kept (the persistent launch won on a batch of 512
+        mixed sizes, the graphs on 32 equal 512^2 images)."""
+        if self._persistent_req is None and self.C == 1:
+            self.persistent = True
+            rp = self._autotune_persistent(iters)
+            tp = dict(self.tuning)
+            gp = self.gran
+            self.persistent = False
+            rg = self._autotune_graphs(iters)
+            tg = dict(self.tuning)
+            if tp["ms_per_iteration"] <= tg["ms_per_iteration"]:
+                self.persistent, self.rows_per_item, self.tuning, self.gran = True, rp, tp, gp
+            self.tuning["mode"] = "persistent" if self.persistent else "graphs"
+            self.tuning["ms_per_iteration_other_mode"] = (
+                tg if self.persistent else tp)["ms_per_iteration"]
+            return self.rows_per_item
+        if self.persistent:
+            return self._autotune_persistent(iters)
+        return self._autotune_graphs(iters)
+
+    def _autotune_graphs(self, iters=4):
         """Rows per work item: each candidate runs `iters` iterations from the
         zero start, timed with CUDA events; the fastest is kept and the state
         reset (the tuning iterations do not count).  With granularity=None
@@ -243,8 +269,6 @@ class BatchROF(object):
         and an instance runs on average g/2 iterations past its stop, so g
         minimises t_gap/g + t_iter g/(2 n) for n = GRAN_PRIOR_ITERS, i.e.
         g = sqrt(2 n t_gap / t_iter), even, within GRAN_RANGE."""
-        if self.persistent:
-            return self._autotune_persistent(iters)
         t = torch()
         best = None
         active = np.ones(self.n, np.uint8)
