@@ -51,33 +51,6 @@ template <typename T> OPYX_D T ld(const T* p) { return __ldg(p); }
 // a reduction buffer can be reused by the next launch on the same stream.
 // ---------------------------------------------------------------------------
 
-// Sums of per-element terms.  FP32 iterates: FP32 partial sums of runs of
-// kAccRun terms, each run added into FP64 -- an FP64 operation per element
-// costs a warp about 16 issue slots of GB300's FP64 pipe, the fold one per
-// run; FP64 iterates: FP64 throughout.
-constexpr int kAccRun = 8;
-template <typename T>
-struct Acc {
-  double s = 0.0;
-  __device__ __forceinline__ void add(T v) { s += (double)v; }
-  __device__ __forceinline__ double get() const { return s; }
-};
-template <>
-struct Acc<float> {
-  double s = 0.0;
-  float p = 0.f;
-  int n = 0;
-  __device__ __forceinline__ void add(float v) {
-    p += v;
-    if (++n == kAccRun) {
-      s += (double)p;
-      p = 0.f;
-      n = 0;
-    }
-  }
-  __device__ __forceinline__ double get() const { return s + (double)p; }
-};
-
 enum RedOp { RED_SUM = 0, RED_MAX = 1 };
 
 OPYX_D double red_apply(int op, double a, double b) {

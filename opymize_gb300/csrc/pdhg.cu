@@ -37,15 +37,15 @@ k_residual_pair(int64_t n, StepT<T> a, const T* __restrict__ zk, const T* __rest
                 T b, const T* __restrict__ zgk, T c1, T c2, const T* __restrict__ zgkp1,
                 double* out, double* partials, unsigned* ticket) {
   a.load();
-  Acc<T> s1, s2;
+  double s1 = 0.0, s2 = 0.0;
   GRID_STRIDE(i, n) {
     const T base = (zk[i] - zkp1[i]) / a.at(i) - b * zgk[i];
-    const T r1 = base + c1 * zgkp1[i];
-    const T r2 = base + c2 * zgkp1[i];
-    s1.add(r1 * r1);
-    s2.add(r2 * r2);
+    const double r1 = (double)(base + c1 * zgkp1[i]);
+    const double r2 = (double)(base + c2 * zgkp1[i]);
+    s1 += r1 * r1;
+    s2 += r2 * r2;
   }
-  double vals[2] = {s1.get(), s2.get()};
+  double vals[2] = {s1, s2};
   const int ops[2] = {RED_SUM, RED_SUM};
   block_reduce_and_finish<2>(vals, ops, partials, ticket, [&](double* tot) {
     out[0] += tot[0];

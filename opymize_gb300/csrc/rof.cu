@@ -313,12 +313,6 @@ struct SweepLaunch {
   static void run(const Geo<T>&, const Args<T>&, cudaStream_t) {}
 };
 
-// Tile width of one-channel sweeps on rows longer than 256 pixels.
-#ifndef OPYX_SWEEP_TW1
-#define OPYX_SWEEP_TW1 512
-#endif
-constexpr int kSweepTW1 = OPYX_SWEEP_TW1;
-
 template <int C>
 struct SweepLaunch<float, 2, C> {
   template <int TW>
@@ -339,7 +333,7 @@ struct SweepLaunch<float, 2, C> {
   // narrow rows get narrow tiles, so that no CTA carries idle threads
   static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
     if (g.nl <= 128) go<128>(g, a, s);
-    else if (g.nl <= 256 || (C == 1 && kSweepTW1 == 256)) go<256>(g, a, s);
+    else if (g.nl <= 256) go<256>(g, a, s);
     else go<kPipeTW>(g, a, s);
   }
 };

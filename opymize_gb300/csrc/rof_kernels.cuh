@@ -264,7 +264,7 @@ OPYX_D T sigma_const(const Args<T>& a, const Geo<T>& g) {
 template <typename T, int D, int C, int ADAPT>
 __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
   if (stopped(a)) return;
-  Acc<T> acc;
+  double acc = 0.0;
   const PrimalCoefs<T, C> pc(g, tau_const(a, g));
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
   ROF_PIXEL_LOOP {
@@ -292,12 +292,12 @@ __global__ void __launch_bounds__(256) k_passA(Geo<T> g, Args<T> a) {
       if (ADAPT) {
         const T gpk = (xo - xn) / tau - div[k];
         a.gp[i * C + k] = gpk;
-        acc.add(gpk * gpk);
+        acc += (double)gpk * (double)gpk;
       }
     }
   }
   if (ADAPT) {
-    double vals[1] = {acc.get()};
+    double vals[1] = {acc};
     const int ops[1] = {RED_SUM};
     opyx_adaptive_state* st = a.st;
     block_reduce_and_finish<1>(vals, ops, a.partials, a.ticket,
@@ -315,7 +315,7 @@ template <typename T, int D, int C, int ADAPT>
 __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
   if (stopped(a)) return;
   constexpr int M = D * C;
-  Acc<T> acc_r, acc_g;
+  double acc_r = 0.0, acc_g = 0.0;
   const T sig_c = sigma_const(a, g);
   const T hub_c = T(1) / (T(1) + sig_c * g.hub_ratio);
   const bool pre = g.steps == OPYX_STEPS_PRECOND;
@@ -351,15 +351,15 @@ __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
         // A x_k from xbar = (1+theta) x_{k+1} - theta x_k
         const T axk = ((T(1) + th) * gn[j] - gb[j]) / th;
         const T base = (yo[j] - yv[j]) / sig[j] - th * axk;
-        const T rr = base + th * gn[j];
-        const T gg = base + (th + T(1)) * gn[j];
-        acc_r.add(rr * rr);
-        acc_g.add(gg * gg);
+        const double rr = (double)(base + th * gn[j]);
+        const double gg = (double)(base + (th + T(1)) * gn[j]);
+        acc_r += rr * rr;
+        acc_g += gg * gg;
       }
     }
   }
   if (ADAPT) {
-    double vals[2] = {acc_r.get(), acc_g.get()};
+    double vals[2] = {acc_r, acc_g};
     const int ops[2] = {RED_SUM, RED_SUM};
     opyx_adaptive_state* st = a.st;
     block_reduce_and_finish<2>(vals, ops, a.partials, a.ticket, [&](double* tot) {
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(256) k_passB(Geo<T> g, Args<T> a) {
 template <typename T, int D, int C, int RESID>
 __global__ void __launch_bounds__(256) k_passR(Geo<T> g, Args<T> a) {
   if (stopped(a)) return;
-  Acc<T> acc;
+  double acc = 0.0;
   ROF_PIXEL_LOOP {
     const int64_t i = r * g.nl + q;
     int64_t c[3];
@@ -386,13 +386,13 @@ __global__ void __launch_bounds__(256) k_passR(Geo<T> g, Args<T> a) {
     for (int k = 0; k < C; ++k) {
       a.xgrad[i * C + k] = div[k];
       if (RESID) {
-        const T rp = a.gp[i * C + k] + div[k];
-        acc.add(rp * rp);
+        const double rp = (double)(a.gp[i * C + k] + div[k]);
+        acc += rp * rp;
       }
     }
   }
   if (RESID) {
-    double vals[1] = {acc.get()};
+    double vals[1] = {acc};
     const int ops[1] = {RED_SUM};
     opyx_adaptive_state* st = a.st;
     block_reduce_and_finish<1>(vals, ops, a.partials, a.ticket, [&](double* tot) {
