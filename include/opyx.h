@@ -209,7 +209,9 @@ int opyx_epigraph_eval(const opyx_epigraph* e, int dtype, int which, const void*
  *   prox_sigmaF* = (q, e, projection of p onto |p_i| <= lbd, s - sigma,
  *                   EpigraphInd projection of every z[j, i] (ndim 1)).
  * which = 0 (pass A): xkp1 = prox(xk - tau A^T yk), xbar = (1+theta) xkp1 -
- * theta xk; which = 1 (pass B): ykp1 = prox(yk + sigma A xbar).  It replaces
+ * theta xk; which = 1 (pass B): ykp1 = prox(yk + sigma A xbar); which = 2:
+ * the envelopes' live lines of every interval instance into `hull` (once per
+ * solve: they depend on the data term only).  It replaces
  * the generic path's chain of BlockOp / IndexedMultAdj / MatrixMultR /
  * ScaleOp / GradientOp and prox launches for this model (about 22 per
  * iteration).  Steps: tau and sigma of u, mu, q, e, s, z per label /
@@ -243,6 +245,10 @@ typedef struct {
   int32_t sorted;                /* perm gives each interval's points by increasing, */
   uint8_t perm[31 * 16];         /* distinct slope (the projection skips its sort)   */
   double vsorted[31 * 16];       /* those slopes, in that order (host copy)          */
+  uint8_t* hull;                 /* (L-1, N) device bytes, or NULL: bit k set if the
+                                    k-th point (increasing slope) carries a piece of
+                                    the instance's envelope; which = 2 fills it (needs
+                                    sorted), pass B then projects over those lines  */
 } opyx_sublabel;
 int opyx_sublabel_pass(const opyx_sublabel* d, int which, void* stream);
 

@@ -90,7 +90,7 @@ class opyx_sublabel(C.Structure):
                 ("sig_p0", C.c_double), ("lbd", C.c_double), ("theta", C.c_double),
                 ("v", C.c_void_p), ("bt", C.c_void_p), ("It", C.c_void_p), ("J", C.c_void_p),
                 ("sorted", C.c_int32), ("perm", C.c_uint8 * (31 * 16)),
-                ("vsorted", C.c_double * (31 * 16))]
+                ("vsorted", C.c_double * (31 * 16)), ("hull", C.c_void_p)]
 
 
 class opyx_rof_problem(C.Structure):

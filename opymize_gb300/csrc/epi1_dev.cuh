@@ -126,5 +126,83 @@ OPYX_D void project1(T (&cv)[NS], T (&cb)[NS], bool (&on)[NS], T s0, T t0, T& ys
   if (!found) { ys = fs; yt = ft; }
 }
 
+// Bit k of the result: line k (of lines sorted by increasing, distinct
+// slope) carries a piece of the envelope g -- the liveness test of project1
+// alone.  It depends only on the lines, so where they stay fixed over many
+// projections it is computed once (project1_live then skips it).
+template <typename T, int NS>
+OPYX_D unsigned live_mask1(const T (&cv)[NS], const T (&cb)[NS], const bool (&on)[NS]) {
+  unsigned mask = 0;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    if (!on[k]) continue;
+    T lo = -T(INFINITY), hi = T(INFINITY);
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      if (m == k || !on[m]) continue;
+      const T sl = (cb[k] - cb[m]) / (cv[k] - cv[m]);
+      if (m < k) lo = fmax(lo, sl);
+      else hi = fmin(hi, sl);
+    }
+    if (!(lo > hi)) mask |= 1u << k;
+  }
+  return mask;
+}
+
+// project1 for lines sorted by increasing, distinct slope whose envelope's
+// pieces are known (bit k of `live`: line k carries one): the scan visits
+// the live lines only, each vertex is the intersection of two consecutive
+// live lines (one division), and the violation is the largest over the live
+// lines (the others lie below the envelope).  Same tests, same order.
+template <typename T, int NS>
+OPYX_D void project1_live(const T (&cv)[NS], const T (&cb)[NS], unsigned live, T s0, T t0, T& ys,
+                          T& yt) {
+  ys = s0;
+  yt = t0;
+  T viol = -T(INFINITY);
+#pragma unroll
+  for (int k = 0; k < NS; ++k)
+    if ((live >> k) & 1u) viol = fmax(viol, cv[k] * s0 - t0 - cb[k]);
+  if (!(viol > T(0))) return;
+  bool found = false, have = false;
+  T pv = T(0), pb = T(0), plo = -T(INFINITY);
+  T best = T(INFINITY), fs = s0, ft = t0;
+  // the inside of the piece of line (v, b) over [lo, hi]
+  auto inside = [&](T v, T b, T lo, T hi) {
+    const T sk = (s0 + v * (t0 + b)) / (T(1) + v * v);
+    const T r = v * s0 - t0 - b;
+    if (r > T(0) && sk >= lo && sk <= hi) {
+      found = true;
+      ys = sk;
+      yt = v * sk - b;
+    } else {
+      const T sc = fmin(fmax(sk, lo), hi), tc = v * sc - b;
+      const T d = (sc - s0) * (sc - s0) + (tc - t0) * (tc - t0);
+      if (d < best) { best = d; fs = sc; ft = tc; }
+    }
+  };
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    if (!((live >> k) & 1u)) continue;
+    if (have) {
+      const T V = (cb[k] - pb) / (cv[k] - pv);   // vertex: hi of the previous piece, lo of this one
+      if (!found) inside(pv, pb, plo, V);
+      if (!found) {
+        const T vt = cv[k] * V - cb[k];
+        const T dl = (V - s0) + pv * (vt - t0), dr = (V - s0) + cv[k] * (vt - t0);
+        if (dl <= T(0) && dr >= T(0)) { found = true; ys = V; yt = vt; }
+        const T d = (V - s0) * (V - s0) + (vt - t0) * (vt - t0);
+        if (d < best) { best = d; fs = V; ft = vt; }
+      }
+      plo = V;
+    }
+    pv = cv[k];
+    pb = cb[k];
+    have = true;
+  }
+  if (!found && have) inside(pv, pb, plo, T(INFINITY));
+  if (!found) { ys = fs; yt = ft; }
+}
+
 }  // namespace epi
 }  // namespace opyx

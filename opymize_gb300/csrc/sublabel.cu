@@ -69,6 +69,7 @@ struct Args {
   uint8_t perm[kLmax - 1][16];     // distinct v (the projection then skips its sort)
   int use_inv;                     // sorted with at most 8 points: inv holds per interval
   T inv[kLmax - 1][36];            // 1/(v_k - v_m) (28 pairs) and 1/(1 + v_k^2) (8)
+  uint8_t* hull;                   // (L - 1, N) live lines of every instance (sorted order), or NULL
 };
 
 // A pixel's L label values (L <= LT) between registers and memory: 128-bit
@@ -200,13 +201,63 @@ OPYX_D void z_project(const Args<T>& a, int j, int64_t i) {
   z_n[o + 1] = yt;
 }
 
+// The z block of interval j at pixel i with the instance's live lines known
+// (hull): only they are read, and the scan visits only them.
+template <typename T, int NS>
+OPYX_D void z_project_live(const Args<T>& a, int j, int64_t i) {
+  const int64_t N = a.N, L = a.L;
+  const T* mub = a.xbar + N * L + N;
+  const T* z_k = a.yk + N * L + 4 * N;
+  T* z_n = a.ykp1 + N * L + 4 * N;
+  const unsigned live = a.hull[j * N + i];
+  T cv[NS], cb[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const bool on = (live >> k) & 1u;
+    const int64_t l = on ? a.J[j * a.nsub + a.perm[j][k]] : 0;
+    cv[k] = on ? a.v[l] : T(0);
+    cb[k] = on ? a.bt[l * N + i] : T(0);
+  }
+  const int64_t o = (j * N + i) * 2;
+  const T s0 = z_k[o] + a.sig_z[j][0] * mub[o];
+  const T t0 = z_k[o + 1] + a.sig_z[j][1] * mub[o + 1];
+  T ys, yt;
+  epi::project1_live<T, NS>(cv, cb, live, s0, t0, ys, yt);
+  z_n[o] = ys;
+  z_n[o + 1] = yt;
+}
+
+// The live lines of every (interval, pixel) instance, once per solve (the
+// data term is fixed): bit k for the k-th point in increasing slope.
+template <typename T, int NS>
+__global__ void __launch_bounds__(kThreads) k_hull(Args<T> a) {
+  const int j = (int)blockIdx.y;
+  SUB_GRID_STRIDE(i, a.N) {
+    T cv[NS], cb[NS];
+    bool on[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const bool used = k < a.nsub;
+      const int64_t l = used ? a.J[j * a.nsub + a.perm[j][k]] : 0;
+      on[k] = used && (!a.It || a.It[l * a.N + i] != 0);
+      cv[k] = on[k] ? a.v[l] : T(0);
+      cb[k] = on[k] ? a.bt[l * a.N + i] : T(0);
+    }
+    a.hull[j * a.N + i] = (uint8_t)epi::live_mask1<T, NS>(cv, cb, on);
+  }
+}
+
 // ---- pass B, z blocks: blockIdx.y = j the interval (a kernel of its own:
 // far fewer registers than the pixel part, so twice the resident warps for
 // this compute-bound part)
 template <typename T, int NS, bool SORTED>
 __global__ void __launch_bounds__(kThreads, 8) k_pass_z(Args<T> a) {
   const int j = (int)blockIdx.y;
-  SUB_GRID_STRIDE(i, a.N) z_project<T, NS, SORTED>(a, j, i);
+  if (SORTED && a.hull) {
+    SUB_GRID_STRIDE(i, a.N) z_project_live<T, NS>(a, j, i);
+  } else {
+    SUB_GRID_STRIDE(i, a.N) z_project<T, NS, SORTED>(a, j, i);
+  }
 }
 
 // ---- pass B, the q, e, p, s blocks of every pixel
@@ -291,6 +342,12 @@ static int launch_l(const Args<T>& a, int which, cudaStream_t s) {
     k_pass_a<T, LT><<<g, kThreads, 0, s>>>(a);
     return check_launch();
   }
+  if (which == 2) {   // the instances' live lines, into a.hull
+    const dim3 grid(g, (unsigned)(a.L - 1), 1);
+    if (a.nsub <= 8) k_hull<T, 8><<<grid, kThreads, 0, s>>>(a);
+    else k_hull<T, 16><<<grid, kThreads, 0, s>>>(a);
+    return check_launch();
+  }
   k_pass_b<T, LT><<<g, kThreads, 0, s>>>(a);
   int st = check_launch();
   if (st) return st;
@@ -344,6 +401,7 @@ static int launch(const opyx_sublabel* d, int which, cudaStream_t s) {
   a.It = d->It;
   a.J = d->J;
   a.sorted = d->sorted;
+  a.hull = d->hull;
   // reciprocals of the sorted points' slope differences (one interval's
   // points are shared by every pixel): the projection multiplies
   a.use_inv = d->sorted && d->nsub <= 8;
@@ -371,12 +429,14 @@ static int launch(const opyx_sublabel* d, int which, cudaStream_t s) {
 using namespace opyx;
 
 extern "C" int opyx_sublabel_pass(const opyx_sublabel* d, int which, void* stream) {
-  if (!d || (which != 0 && which != 1)) return OPYX_ERR_ARG;
+  if (!d || which < 0 || which > 2) return OPYX_ERR_ARG;
+  if (which == 2 && (!d->hull || !d->sorted)) return OPYX_ERR_ARG;
   if (d->H < 1 || d->W < 1 || d->nsub < 2 || d->nsub > 16) return OPYX_ERR_ARG;
   if (d->L < 2 || d->L > 32) return OPYX_ERR_UNSUPPORTED;
-  if (!d->xk || !d->xbar || !d->yk || (which == 0 && !d->xkp1) || (which == 1 && !d->ykp1))
+  if (which < 2 && (!d->xk || !d->xbar || !d->yk || (which == 0 && !d->xkp1) ||
+                    (which == 1 && !d->ykp1)))
     return OPYX_ERR_ARG;
-  if (which == 1 && (!d->v || !d->bt || !d->J)) return OPYX_ERR_ARG;
+  if (which >= 1 && (!d->v || !d->bt || !d->J)) return OPYX_ERR_ARG;
   if (d->sorted)
     for (int j = 0; j < d->L - 1; ++j)
       for (int k = 0; k < d->nsub; ++k)

@@ -113,6 +113,12 @@ class SublabelPasses(object):
         self.d = d
         self.xbar = DeviceArray.empty((N * (L + 1) + (L - 1) * N * 2,), dtype)
         d.xbar = self.xbar.ptr
+        if d.sorted:
+            # which lines carry the envelope of every instance: fixed by the
+            # data term, so found once; the projections then scan only those
+            self.hull = DeviceArray.empty(((L - 1) * N,), np.uint8)
+            d.hull = self.hull.ptr
+            _lib.call("opyx_sublabel_pass", d, 2, stream_ptr())
 
     def iterate(self, v):
         """One iteration: x_{k+1} into v['xkp1'], y_{k+1} into v['ykp1']."""
