@@ -12,7 +12,8 @@
 //
 // A warp owns a strip of 128 pixels (4 per lane) and a run of rows, and
 // needs nothing from other warps: the rows arrive by 128-bit loads straight
-// into registers, one row ahead of their use; y_k and xbar of the previous
+// into registers, two rows ahead of their use (one row ahead: 0.82 against
+// 0.76 ms per iteration of the 512-instance batch); y_k and xbar of the previous
 // row stay in registers; neighbours along the row come by warp shuffles,
 // and only lane 0 (the y value left of the strip) and lane 31 (pass A of
 // the pixel right of it, for pass B's neighbour) load a few scalars more.
@@ -174,6 +175,11 @@ OPYX_D Row1 load_row1(const Geo<float>& g, const Args<float>& a, int64_t r, int6
 // q_beg (clipped to the image), by one warp: lane l owns the quad at
 // q_beg + 4 l.  Reads a.x, a.y, a.f; writes a.x2, a.y2.  MASK: a.mask is
 // set (else the SSD term applies everywhere).
+#ifndef OPYX_STRIP_PF
+#define OPYX_STRIP_PF 2
+#endif
+constexpr int kStripPF = OPYX_STRIP_PF;   // rows each lane has in flight
+
 template <bool PRE, bool MASK>
 OPYX_D void sweep_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t r0,
                          int64_t r1) {
@@ -198,8 +204,11 @@ OPYX_D void sweep_strip1(const Geo<float>& g, const Args<float>& a, int64_t q_be
 #pragma unroll
   for (int p = 0; p < 4; ++p) pxb[p] = 0.f;
   Row1 cur = load_row1<MASK>(g, a, r0, q0, act, lane);
+  Row1 nx2 = load_row1<MASK>(g, a, kStripPF > 1 && r0 + 1 <= rl ? r0 + 1 : -1, q0, act, lane);
   for (int64_t r = r0; r <= r1; ++r) {
-    const Row1 nxt = load_row1<MASK>(g, a, r + 1 <= rl ? r + 1 : -1, q0, act, lane);
+    const Row1 nxt = kStripPF > 1 ? nx2
+                                  : load_row1<MASK>(g, a, r + 1 <= rl ? r + 1 : -1, q0, act, lane);
+    if (kStripPF > 1) nx2 = load_row1<MASK>(g, a, r + 2 <= rl ? r + 2 : -1, q0, act, lane);
     const bool has_up = r > 0, has_dn = r < g.rows - 1;
     const float cy0[4] = {cur.y01.x, cur.y01.z, cur.y23.x, cur.y23.z};
     const float cy1[4] = {cur.y01.y, cur.y01.w, cur.y23.y, cur.y23.w};
