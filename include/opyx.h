@@ -596,6 +596,16 @@ int opyx_rof_iterate_noalloc(const opyx_rof_problem* p, void* x, void* y, const 
 /* Primal-dual gap of the current iterate into the workspace's info record
  * (FP64 device reductions; pdhg.py:23-44, :287-305). */
 int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* stream);
+/* opyx_rof_gap followed by opyx_rof_iterate(iters): the check at the end of
+ * one granularity chunk (pdhg.py:285-305) queued with the iterations of the
+ * next.  With single sweeps (iters >= 2) the first sweep computes the gap of
+ * the state it reads from the rows it loads anyway -- no pass over HBM of its
+ * own -- and writes its iteration into the second buffers, so when the stop
+ * test passes, x and y keep the checked state and the later launches return
+ * at once, as after the two calls.  The info record then equals the two
+ * calls' up to the order of the FP64 sums. */
+int opyx_rof_gap_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                         void* stream);
 
 
 /* ---- Learned warm start: U-Net kernels (BF16 tensor cores, FP32 accumulation) ----

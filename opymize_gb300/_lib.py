@@ -187,6 +187,7 @@ SIGNATURES = {
     "opyx_rof_init": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), vp]),
     "opyx_rof_iterate": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), i32, vp]),
     "opyx_rof_gap": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), vp]),
+    "opyx_rof_gap_iterate": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), i32, vp]),
     "opyx_rof_pass": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers), i32, vp]),
     "opyx_rof_uses_sweep": (i32, [P(opyx_rof_problem), P(opyx_rof_buffers)]),
     "opyx_rof_iterate_noalloc": (i32, [P(opyx_rof_problem), vp, vp, vp, vp, i32, vp, vp]),

@@ -311,30 +311,42 @@ static bool sweep_ok(const opyx_rof_problem* p, const opyx_rof_buffers* b) {
 template <typename T, int D, int C>
 struct SweepLaunch {
   static void run(const Geo<T>&, const Args<T>&, cudaStream_t) {}
+  static bool run_gap(const Geo<T>&, const Args<T>&, double, cudaStream_t) { return false; }
 };
 
 template <int C>
 struct SweepLaunch<float, 2, C> {
-  template <int TW>
-  static void go(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
+  // GAP: the sweep that also computes the gap of its input state; false if
+  // its grid would need more CTAs than the reduction has partials for.
+  template <int TW, bool GAP>
+  static bool go(const Geo<float>& g, const Args<float>& a, double shift, cudaStream_t s) {
     constexpr int P = sweep_p(C), DP = sweep_depth(C);
     constexpr int smem = SweepSmem<C, TW, DP>::bytes;
     static int per_sm = -1;
-    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C, TW, P, DP>, smem, TW / P);
+    if (per_sm < 0) per_sm = pipe_blocks_per_sm(k_sweep<C, TW, P, DP, GAP>, smem, TW / P);
     const int64_t gx = (g.nl + TW - 1) / TW;
-    const int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
+    int64_t target = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
+    if (GAP && target > kMaxBlocks) target = kMaxBlocks;
     int64_t gy = target / gx;
     if (gy < 1) gy = 1;
     if (gy > g.rows) gy = g.rows;
     const int RB = (int)((g.rows + gy - 1) / gy);
     gy = (g.rows + RB - 1) / RB;
-    k_sweep<C, TW, P, DP><<<dim3((unsigned)gx, (unsigned)gy, 1), TW / P, smem, s>>>(g, a, RB);
+    if (GAP && gx * gy > kMaxBlocks) return false;
+    launch_chained(k_sweep<C, TW, P, DP, GAP>, dim3((unsigned)gx, (unsigned)gy, 1), dim3(TW / P),
+                   smem, s, g, a, RB, shift);
+    return true;
   }
   // narrow rows get narrow tiles, so that no CTA carries idle threads
   static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
-    if (g.nl <= 128) go<128>(g, a, s);
-    else if (g.nl <= 256) go<256>(g, a, s);
-    else go<kPipeTW>(g, a, s);
+    if (g.nl <= 128) go<128, false>(g, a, 0.0, s);
+    else if (g.nl <= 256) go<256, false>(g, a, 0.0, s);
+    else go<kPipeTW, false>(g, a, 0.0, s);
+  }
+  static bool run_gap(const Geo<float>& g, const Args<float>& a, double shift, cudaStream_t s) {
+    if (g.nl <= 128) return go<128, true>(g, a, shift, s);
+    if (g.nl <= 256) return go<256, true>(g, a, shift, s);
+    return go<kPipeTW, true>(g, a, shift, s);
   }
 };
 
@@ -371,8 +383,9 @@ struct SweepLaunch<float, 3, C> {
     const int ZC = (int)((Z + best_nc - 1) / best_nc);
     const int64_t items = (int64_t)nyt * ((Z + ZC - 1) / ZC);
     const int64_t grid = items < R ? items : R;
-    k_sweep3<TW, TY, P><<<(unsigned)grid, threads, smem, s>>>(g, a, ZC, nyt);
+    launch_chained(k_sweep3<TW, TY, P>, dim3((unsigned)grid), dim3(threads), smem, s, g, a, ZC, nyt);
   }
+  static bool run_gap(const Geo<float>&, const Args<float>&, double, cudaStream_t) { return false; }
   static void run(const Geo<float>& g, const Args<float>& a, cudaStream_t s) {
     if (C != 1) return;
     if (g.nl == 128) go<128>(g, a, s);
@@ -478,6 +491,27 @@ struct Runner {
     launch(p, g, a, 3, vec_ok<T>(p, b), rows_per_thread(p, g), s, pipe_ok<T>(p, b));
     return check_launch();
   }
+
+  // The gap of the current state, then `iters` iterations.  With single
+  // sweeps the first sweep computes the gap from the rows it reads (into
+  // the second buffers, so a passing stop test leaves (x, y) as checked and
+  // the remaining launches return at once); else opyx_rof_gap first.
+  static int gap_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                         cudaStream_t s) {
+    if (iters >= 2 && sweep_ok<T, D>(p, b)) {
+      Geo<T> g = make_geo<T>(p);
+      Args<T> a = make_args<T>(p, b);
+      if (SweepLaunch<T, D, C>::run_gap(g, a, p->ssd_shift, s)) {
+        SweepLaunch<T, D, C>::run(g, swapped(a), s);
+        int st = check_launch();
+        if (st) return st;
+        return iterate(p, b, iters - 2, s);
+      }
+    }
+    int st = gap(p, b, s);
+    if (st) return st;
+    return iterate(p, b, iters, s);
+  }
 };
 
 template <typename F>
@@ -571,6 +605,15 @@ int opyx_rof_gap(const opyx_rof_problem* p, const opyx_rof_buffers* b, void* str
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   return dispatch(p, [&](auto r) { return decltype(r)::gap(p, b, s); });
+}
+
+int opyx_rof_gap_iterate(const opyx_rof_problem* p, const opyx_rof_buffers* b, int iters,
+                         void* stream) {
+  int st = validate(p, b);
+  if (st) return st;
+  if (iters < 0) return OPYX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dispatch(p, [&](auto r) { return decltype(r)::gap_iterate(p, b, iters, s); });
 }
 
 }  // extern "C"

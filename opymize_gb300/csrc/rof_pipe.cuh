@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(TW / 4) k_passA_p(Geo<float> g, Args<float> a,
 
 // ------------------------------------------------------------------ gap
 // The sums of k_gap; FP32 partials per thread over its pixels and rows,
-// FP64 across threads and blocks.
+// double-float pairs across runs and threads, FP64 across blocks.
 template <int D, int C, int TW = kPipeTW>
 __global__ void __launch_bounds__(TW / 4) k_gap_p(Geo<float> g, Args<float> a, int RB,
                                                         double ssd_shift) {
@@ -313,7 +313,8 @@ __global__ void __launch_bounds__(TW / 4) k_gap_p(Geo<float> g, Args<float> a, i
   const int64_t q_beg = blockIdx.x * (int64_t)TW;
   const int lp0 = threadIdx.x * 4;
   const int64_t nplane = D == 3 ? g.n[1] : 0;
-  double sG = 0.0, sF = 0.0, sGs = 0.0, sFs = 0.0, inf = 0.0;
+  DF sum[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};   // runs so far
+  float inf = 0.f;
   for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
     const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
     float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;
@@ -421,15 +422,13 @@ __global__ void __launch_bounds__(TW / 4) k_gap_p(Geo<float> g, Args<float> a, i
     }
     cp_wait<0>();
     __syncthreads();
-    sG += 0.5 * (double)pG;
-    sF += (double)pF;
-    sGs += (double)pGs;
-    sFs += (double)pFs;
-    inf = fmax(inf, (double)pinf);
+    sum[0] = df_add(sum[0], DF{0.5f * pG, 0.f});
+    sum[1] = df_add(sum[1], DF{pF, 0.f});
+    sum[2] = df_add(sum[2], DF{pGs, 0.f});
+    sum[3] = df_add(sum[3], DF{pFs, 0.f});
+    inf = fmaxf(inf, pinf);
   }
-  double vals[5] = {sG, sF, sGs, sFs, inf};
-  const int ops[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
-  block_reduce_and_finish<5>(vals, ops, a.partials, a.ticket, [&](double* tot) {
+  block_reduce_df_and_finish<4>(sum, inf, a.partials, a.ticket, [&](double* tot) {
     write_info(g, a, tot, ssd_shift);
   });
 }

@@ -249,15 +249,138 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
   bulk_commit();
 }
 
+// The primal-dual gap of the state a sweep starts from (x_k, y_k), summed
+// from the rows the sweep has in shared memory anyway: at row step r the
+// terms of row r that need only rows r - 1 and r (G(x), G*(-A^T y), |y|^2,
+// the infeasibility, the horizontal part of |A x|^2), and the vertical part of
+// row r - 1 from x_k of rows r - 1 (kept in registers) and r.  The per-pixel
+// arithmetic is that of k_gap_p; FP32 sums per thread over its run, FP64
+// across threads and CTAs (the last CTA folds them and runs the stop test).
+template <int C, int P>
+struct SweepGap {
+  float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;   // this run
+  DF sum[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};      // runs so far
+  float xp[P * C];   // x_k of the previous row at this thread's pixels
+  float hp[P];       // horizontal |A x|^2 of the previous row
+  OPYX_D void fold_run() {
+    sum[0] = df_add(sum[0], DF{0.5f * pG, 0.f});
+    sum[1] = df_add(sum[1], DF{pF, 0.f});
+    sum[2] = df_add(sum[2], DF{pGs, 0.f});
+    sum[3] = df_add(sum[3], DF{pFs, 0.f});
+    pG = pF = pGs = pFs = 0.f;
+  }
+};
+
+// Square root for the gap sums: the hardware approximation (sqrt.approx.f32,
+// relative error about 2^-23); the sums it enters carry FP32 rounding of the
+// same size, and the IEEE-rounded sqrtf doubled the instructions of the row
+// step.
+OPYX_D float gap_sqrt(float v) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
+// |A x|^2 of pixel p of the previous row is complete: its F term.
+template <int C, int P>
+OPYX_D void gap_f_term(const Geo<float>& g, SweepGap<C, P>& acc, float n2) {
+  const float nrm = gap_sqrt(n2);
+  acc.pF += g.use_huber ? (nrm <= g.huber ? n2 * g.half_rhuber : nrm - g.half_huber) : nrm;
+}
+
+// Row step r of a run [r0, r1) with x_k row r in `xv` (not yet overwritten
+// by x_{k+1}), y_k rows r and r - 1 in `yc`, `yu`, f row r in `fv`; called
+// by every thread of the CTA (warp shuffles).  Finishes row r - 1 (r > r0)
+// and, for r < r1, sums the terms of row r.  Pixel tests in tile-local
+// 32-bit indices: nq pixels of the tile lie in the image, the first lx have a
+// right neighbour.
+template <int C, int P>
+OPYX_D void gap_row(const Geo<float>& g, const Args<float>& a, const float* yc, const float* yu,
+                    const float* xv, const float* fv, int64_t r, int64_t r0, int64_t r1,
+                    int64_t q_beg, int lp0, int nq, int lx, SweepGap<C, P>& acc) {
+  constexpr int D = 2, M = D * C;
+  const int lane = threadIdx.x & 31;
+  float qx[P * C], xr[C];
+  lds(qx, xv + lp0 * C);
+#pragma unroll
+  for (int k2 = 0; k2 < C; ++k2) {
+    const float dn = __shfl_down_sync(0xffffffffu, qx[k2], 1);
+    xr[k2] = lane < 31 ? dn : xv[(lp0 + P) * C + k2];
+  }
+  if (r > r0) {
+    // row r - 1 has row r below it
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      float n2 = acc.hp[p];
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) {
+        const float gr = g.coef[D - 2][k2] * (qx[p * C + k2] - acc.xp[p * C + k2]);
+        n2 = fmaf(gr, gr, n2);
+      }
+      if (lp0 + p < nq) gap_f_term(g, acc, n2);
+    }
+  }
+  if (r >= r1) return;
+  float qy[P * M], qu[P * M], qf[P * C], yl[C];
+  lds(qy, yc + (lp0 + 4) * M);
+  lds(qu, yu + (lp0 + 4) * M);
+  lds(qf, fv + lp0 * C);
+#pragma unroll
+  for (int k2 = 0; k2 < C; ++k2) {
+    const float up = __shfl_up_sync(0xffffffffu, qy[(P - 1) * M + (D - 1) * C + k2], 1);
+    yl[k2] = lane ? up : yc[(lp0 + 3) * M + (D - 1) * C + k2];
+  }
+  const bool has_up = r > 0, has_dn = r < g.rows - 1;
+  const uint8_t* mrow = a.mask ? a.mask + r * g.nl + q_beg : nullptr;
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    const int lq = lp0 + p;
+    const bool in = lq < nq, inx = lq < lx, has_l = q_beg + lq > 0;
+    const bool on = in && (!mrow || mrow[lq]);
+    float h2 = 0.f, y2 = 0.f;
+#pragma unroll
+    for (int k2 = 0; k2 < C; ++k2) {
+      const float xk = qx[p * C + k2], fk = qf[p * C + k2];
+      const float ihl = g.invh[D - 1], ihr = g.invh[D - 2];
+      float s = inx ? -qy[p * M + (D - 1) * C + k2] * ihl : 0.f;
+      if (has_l) s = fmaf(p > 0 ? qy[(p - 1) * M + (D - 1) * C + k2] : yl[k2], ihl, s);
+      if (has_dn) s = fmaf(-qy[p * M + (D - 2) * C + k2], ihr, s);
+      if (has_up) s = fmaf(qu[p * M + (D - 2) * C + k2], ihr, s);
+      const float ak = g.w[k2] * s;
+      if (on) {
+        const float d = xk - fk;
+        acc.pG = fmaf(g.vol[k2] * d, d, acc.pG);
+        acc.pGs = fmaf(ak, fmaf(ak, g.half_rvol[k2], -fk), acc.pGs);
+      }
+      const float nb = p < P - 1 ? qx[(p + 1) * C + k2] : xr[k2];
+      const float gl = inx ? g.coef[D - 1][k2] * (nb - xk) : 0.f;
+      h2 = fmaf(gl, gl, h2);
+    }
+#pragma unroll
+    for (int j = 0; j < M; ++j) y2 = fmaf(qy[p * M + j], qy[p * M + j], y2);
+    if (in) {
+      acc.pFs += y2;
+      acc.pinf = fmaxf(acc.pinf, gap_sqrt(y2) - g.lbd);
+      if (!has_dn) gap_f_term(g, acc, h2);   // the last row of the image: no vertical part
+    }
+    acc.hp[p] = h2;
+  }
+#pragma unroll
+  for (int j = 0; j < P * C; ++j) acc.xp[j] = qx[j];
+}
+
 // One run of rows [r0, r1) of the column tile [q_beg, q_end) (at most TW
 // pixels): the body of the sweep, shared by the single-instance and the
 // batched kernels.  Pixels of the slot past q_end are computed from the
 // loaded rows but not stored (their own tile stores them).  `st` counts the
 // stages this CTA has issued on its mbarriers.  Returns false if a copy did
 // not arrive within the wait bound (info->fault is then set).
-template <int C, int TW, int P, int DP>
+// GAP: also sum the gap of the state it starts from into *gap (single-image
+// tiles only: q_end = g.nl).
+template <int C, int TW, int P, int DP, bool GAP = false>
 OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg, int64_t q_end,
-                       int64_t r0, int64_t r1, uint64_t* mbar, unsigned& st, float* sm) {
+                       int64_t r0, int64_t r1, uint64_t* mbar, unsigned& st, float* sm,
+                       SweepGap<C, P>* gap = nullptr) {
   using S = SweepSmem<C, TW, DP>;
   constexpr int D = 2, M = D * C, NT = TW / P, NB = DP + 1;
   float* ys = sm;                          // NY x Y44: row q in slot (q - r0 + 1) % NY
@@ -272,6 +395,9 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
   const float sig_c = (float)a.sigma;
   const float hub_c = 1.f / (1.f + sig_c * g.hub_ratio);
   const int64_t rl = r1 < g.rows ? r1 : r1 - 1;   // last row whose pass A runs here
+  // pixels of the tile in the image / with a right neighbour (gap sums)
+  const int gap_nq = (int)(g.nl - q_beg < TW ? g.nl - q_beg : TW);
+  const int gap_lx = (int)(g.nl - 1 - q_beg < TW ? g.nl - 1 - q_beg : TW);
   // stage of row q (r0 <= q <= rl) is base + (q - r0), on mbar[stage % NB]
   const unsigned base = st;
   if (lead) {
@@ -322,6 +448,9 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
     const float* bu = bs + ((k + 1) & 1) * S::X4;         // xbar row r - 1
     // ---- pass A, row r (and xbar at the first pixel past the tile)
     if (run_a) {
+      // (both read shared memory only; the gap first, so that its arrays
+      // and pass A's are not live at once)
+      if (GAP) gap_row<C, P>(g, a, yc, yu, xv, fv, r, r0, r1, q_beg, lp0, gap_nq, gap_lx, *gap);
       float qx[P * C], qb[P * C];
       sweep_a<C, P>(g, a, pc, pre, yc, yu, xv, fv, r, q_beg, lp0, qx, qb);
       float hb[C];
@@ -394,13 +523,15 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
     __syncthreads();
   }
   st = base + (unsigned)(rl - r0 + 1);
+  if (GAP) gap->fold_run();
   return true;
 }
 
-template <int C, int TW = kPipeTW, int P = kSweepP, int DP = 1>
+// GAP: the first sweep of a check chunk, which also computes the gap of the
+// state it reads (opyx_rof_gap_iterate) and runs the stop test on it.
+template <int C, int TW = kPipeTW, int P = kSweepP, int DP = 1, bool GAP = false>
 __global__ void __launch_bounds__(TW / P, sweep_min_blocks(TW, P))
-k_sweep(Geo<float> g, Args<float> a, int RB) {
-  if (stopped(a)) return;
+k_sweep(Geo<float> g, Args<float> a, int RB, double ssd_shift) {
   extern __shared__ float4 smem4[];
   __shared__ __align__(8) uint64_t mbar[kSweepMaxBars];
   float* sm = reinterpret_cast<float*>(smem4);
@@ -410,13 +541,31 @@ k_sweep(Geo<float> g, Args<float> a, int RB) {
     for (int i = 0; i < kSweepMaxBars; ++i) mbar_init(&mbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // launched chained: the previous kernel may still be draining until here
+  chain_wait();
+  if (stopped(a)) return;
   __syncthreads();
   unsigned st = 0;   // stages issued so far; stage s uses mbar[s % (DP+1)]
-  for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
-    const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
-    if (!sweep_rows<C, TW, P, DP>(g, a, q_beg, g.nl, r0, r1, mbar, st, sm)) return;
+  if constexpr (!GAP) {
+    for (int64_t r0 = blockIdx.y * (int64_t)RB; r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
+      const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
+      if (!sweep_rows<C, TW, P, DP>(g, a, q_beg, g.nl, r0, r1, mbar, st, sm)) return;
+    }
+    if (lead) bulk_wait_all();   // the stores have left shared memory and landed
+  } else {
+    SweepGap<C, P> acc;
+    bool ok = true;
+    for (int64_t r0 = blockIdx.y * (int64_t)RB; ok && r0 < g.rows; r0 += (int64_t)gridDim.y * RB) {
+      const int64_t r1 = r0 + RB < g.rows ? r0 + RB : g.rows;
+      ok = sweep_rows<C, TW, P, DP, true>(g, a, q_beg, g.nl, r0, r1, mbar, st, sm, &acc);
+    }
+    if (ok && lead) bulk_wait_all();
+    // every CTA takes part (also one whose copies timed out: the fault flag
+    // is then set and the record is not used), so the ticket completes;
+    // the infeasibility max(|y| - lbd) is taken with 0 as k_gap_p does
+    block_reduce_df_and_finish<4>(acc.sum, fmaxf(acc.pinf, 0.f), a.partials, a.ticket,
+                                  [&](double* tot) { write_info(g, a, tot, ssd_shift); });
   }
-  if (lead) bulk_wait_all();   // the stores have left shared memory and landed
 }
 
 }  // namespace rof

@@ -84,7 +84,6 @@ OPYX_D void store_rows(float* arr, const float* slot, const Geo<float>& g, int64
 template <int TW, int TY, int P>
 __global__ void __launch_bounds__((TY + 1) * (TW / P))
 k_sweep3(Geo<float> g, Args<float> a, int ZC, int nyt) {
-  if (stopped(a)) return;
   using S = Sweep3Smem<TW, TY>;
   constexpr int M = 3, NTR = TW / P, NB = 2;
   extern __shared__ float4 smem4[];
@@ -107,6 +106,9 @@ k_sweep3(Geo<float> g, Args<float> a, int ZC, int nyt) {
     for (int i = 0; i < NB; ++i) mbar_init(&mbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // launched chained: the previous kernel may still be draining until here
+  chain_wait();
+  if (stopped(a)) return;
   __syncthreads();
   unsigned st = 0;
   const int64_t nzc = (Z + ZC - 1) / ZC;

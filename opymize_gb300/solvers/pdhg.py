@@ -462,15 +462,20 @@ class _AdaptiveState(object):
 class _FusedLoop(object):
     """Fused iterations queued ahead of their checks.
 
-    A check chunk is `granularity` iterations and the gap kernel (one CUDA
-    graph per chunk length), then an asynchronous copy of the info record into
-    a pinned host slot and an event.  The host reads a record only when
-    `depth` newer chunks are queued behind it, so the GPU does not idle on the
-    host round trip.  The device-side stop test (term_mode of the problem)
-    makes every kernel queued after the passing check return at once, so
-    state, info and iteration count equal those of a loop that waits at every
-    check, as the reference's does (opymize/solvers/pdhg.py:285-313).
-    `run` must follow opyx_rof_init, which clears the check counter.
+    A check is the gap kernel after `granularity` iterations, then an
+    asynchronous copy of the info record into a pinned host slot and an event.
+    The host reads a record only when `depth` newer ones are queued behind it,
+    so the GPU does not idle on the host round trip.  The device-side stop test
+    (term_mode of the problem) makes every kernel queued after the passing
+    check return at once, so state, info and iteration count equal those of a
+    loop that waits at every check, as the reference's does
+    (opymize/solvers/pdhg.py:285-313).  With single sweeps and no per-check
+    callback, a check is queued with the next chunk's iterations
+    (opyx_rof_gap_iterate: the first sweep computes it from the rows it loads)
+    and its record copied after that chunk; the record then arrives one chunk
+    later, so one fewer newer record is waited for.  Chunks are replayed as
+    CUDA graphs (one per kind and length).  `run` must follow opyx_rof_init,
+    which clears the check counter.
     """
     DEPTH = 2
 
@@ -482,17 +487,20 @@ class _FusedLoop(object):
         self.host = None
         self.launches = 0      # kernel launches queued so far
         self.sweeps = bool(_lib.load().opyx_rof_uses_sweep(p, b))
+        # 2-D sweeps compute a check in their first sweep (3-D: the gap kernel)
+        self.fused_gap = self.sweeps and p.ndim == 2
 
-    def chunk(self, n, check):
-        if check and self.use_graph:
-            g = self.graphs.get(n)
+    def chunk(self, n, check, first=False):
+        """n iterations; `check`: the gap after them; `first`: the gap of the
+        state before them, fused into their first sweep (n >= 2)."""
+        if n and self.use_graph:
+            key = (n, check, first)
+            g = self.graphs.get(key)
             if g is None:
-                g = self.graphs[n] = _RofGraph(self.p, self.b, n)
+                g = self.graphs[key] = _RofGraph(self.p, self.b, n, check, first)
             g.launch()
         else:
-            _lib.call("opyx_rof_iterate", self.p, self.b, n, stream_ptr())
-            if check:
-                _lib.call("opyx_rof_gap", self.p, self.b, stream_ptr())
+            _RofGraph.queue(self.p, self.b, n, check, first, stream_ptr())
         p = self.p
         if self.sweeps:
             kernels = (n // 2) * 2 + (n % 2) * 2       # sweeps; an odd count ends two-pass
@@ -510,6 +518,8 @@ class _FusedLoop(object):
         nrec = len(_lib.ROF_INFO_FIELDS)
         if self.host is None or self.host.shape[0] < depth + 1:
             self.host = t.empty((depth + 1, nrec), dtype=t.float64, pin_memory=True)
+        fuse = self.fused_gap and depth > 0
+        wait_depth = depth - 1 if fuse else depth
         names = _lib.ROF_INFO_FIELDS
         i_checks, i_done, i_fault = names.index("checks"), names.index("done"), names.index("fault")
         pending = []          # (event, slot) of queued checks, oldest first
@@ -530,24 +540,43 @@ class _FusedLoop(object):
                     on_check(rec, check_iters[c - 1])
             return rec[i_done] != 0.0
 
+        def queue_record(at):
+            slot = len(check_iters) % (depth + 1)
+            check_iters.append(at)
+            self.host[slot].copy_(self.info_dev, non_blocking=True)
+            ev = t.cuda.Event()
+            ev.record()
+            pending.append((ev, slot))
+            return read_oldest() if len(pending) > wait_depth else False
+
         it, done = 0, False
+        owed = None           # iteration of a check not queued yet (fused mode)
         while it < maxiter and not done:
             n = min(self.gran - (it % self.gran), maxiter - it)
+            first = owed is not None and n >= 2
+            if owed is not None and not first:
+                self.chunk(0, True)
+                done = queue_record(owed)
+                owed = None
+                if done:
+                    break
             it += n
             stop = interrupted is not None and bool(interrupted())
             check = it % self.gran == 0 or stop
-            self.chunk(n, check)
+            self.chunk(n, check and not fuse, first)
+            if first:
+                done = queue_record(owed) or done
+                owed = None
             if check:
-                slot = len(check_iters) % (depth + 1)
-                check_iters.append(it)
-                self.host[slot].copy_(self.info_dev, non_blocking=True)
-                ev = t.cuda.Event()
-                ev.record()
-                pending.append((ev, slot))
-                if len(pending) > depth:
-                    done = read_oldest()
+                if fuse:
+                    owed = it
+                else:
+                    done = queue_record(it) or done
             if stop:
                 break
+        if owed is not None and not done:
+            self.chunk(0, True)
+            queue_record(owed)
         while pending:
             done = read_oldest() or done
         rec = state["rec"]
@@ -584,18 +613,26 @@ class _GenericGraph(object):
 
 
 class _RofGraph(object):
-    """`n` fused iterations followed by the gap kernel, captured once into a
-    CUDA graph (on a private capture stream) and replayed on the current
-    stream."""
+    """A chunk of fused iterations with its checks -- `first`: the gap of the
+    state before them fused into their first sweep; `check`: the gap kernel
+    after them -- captured once into a CUDA graph (on a private capture
+    stream) and replayed on the current stream."""
 
-    def __init__(self, p, b, n):
+    def __init__(self, p, b, n, check=True, first=False):
         t = torch()
         self.stream = t.cuda.Stream()
         self.graph = t.cuda.CUDAGraph()
         self.stream.wait_stream(t.cuda.current_stream())
         with t.cuda.graph(self.graph, stream=self.stream):
-            s = t.cuda.current_stream().cuda_stream
+            self.queue(p, b, n, check, first, t.cuda.current_stream().cuda_stream)
+
+    @staticmethod
+    def queue(p, b, n, check, first, s):
+        if first:
+            _lib.call("opyx_rof_gap_iterate", p, b, n, s)
+        elif n:
             _lib.call("opyx_rof_iterate", p, b, n, s)
+        if check:
             _lib.call("opyx_rof_gap", p, b, s)
 
     def launch(self):

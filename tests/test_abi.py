@@ -184,6 +184,8 @@ ERROR_CASES = [
     ("opyx_rof_init", (_rof((2 ** 21, 2 ** 21, 2 ** 21)), _rof_buffers(), None), ARG),
     ("opyx_rof_init", (_rof((2 ** 20, 2 ** 19), C=4), _rof_buffers(), None), ARG),  # > 2^40 values
     ("opyx_rof_init", (_rof((0, 4)), _rof_buffers(), None), ARG),
+    ("opyx_rof_gap_iterate", (_rof((64, 64)), _rof_buffers(), -1, None), ARG),
+    ("opyx_rof_gap_iterate", (_rof((2 ** 62 + 1, 4)), _rof_buffers(), 2, None), ARG),
     ("opyx_rof_iterate_noalloc", (_rof((2 ** 62 + 1, 4)), _P, _P, _P, None, 1, None, None),
      _lib.OPYX_ERR_SCRATCH_LIMIT),
     ("opyx_rof_iterate_noalloc", (_rof((4096, 4096)), _P, _P, _P, None, 1, None, None),

@@ -33,6 +33,7 @@ def solve(d, tol, precision="double", waits=False, graph=True, maxiter=100000, *
     G, F, A = gpu_problem(d)
     s = PDHG(G, F, A)
     cb = (lambda state, info: None) if waits else None
+    np.random.seed(0)      # constant steps come from normest's random draws
     s.solve(steps=str(d["steps"]), precision=precision, term_pd_gap=tol,
             term_maxiter=maxiter, granularity=int(d["gran"]), cbfun=cb, graph=graph, **kw)
     assert s.path == "fused"
