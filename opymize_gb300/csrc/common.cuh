@@ -226,30 +226,52 @@ OPYX_D float warp_max_f(float v) {
   return v;
 }
 
+// Arrival of a block at a reduction whose last block folds the partials:
+// `tickets` holds 1 + kTicketGroups zeroed counters.  Blocks count in
+// kTicketGroups groups (bid % kTicketGroups) and the last of each group in
+// tickets[0], so no counter takes more than ~nblocks / 32 atomics (one
+// counter for ~900 blocks, as the sweep's grid has, cost several us of
+// serialised atomics at the end of the kernel).  Called by one thread per
+// block after its partials are written; true for the last block overall,
+// which then resets every counter.
+constexpr int kTicketGroups = 32;
+
+OPYX_D bool arrive_grouped(unsigned* tickets, unsigned bid, unsigned nblocks) {
+  const unsigned ng = nblocks < (unsigned)kTicketGroups ? nblocks : (unsigned)kTicketGroups;
+  const unsigned g = bid % ng;
+  const unsigned in_g = nblocks / ng + (g < nblocks % ng ? 1u : 0u);
+  __threadfence();
+  if (atomicAdd(&tickets[1 + g], 1u) != in_g - 1) return false;
+  __threadfence();
+  if (atomicAdd(&tickets[0], 1u) != ng - 1) return false;
+  __threadfence();
+  for (unsigned j = 0; j <= ng; ++j) tickets[j] = 0u;
+  return true;
+}
+
 // As block_reduce_and_finish for NS sums given as double-float pairs and one
-// maximum given in FP32 (partials and totals in the order sums..., max):
-// the block's sums stay double-float, each block's partial leaves as
-// double(hi) + double(lo), and the last block folds the partials in FP64.
+// maximum given in FP32: each block's partials (sums, then the max) are
+// stored as FP32 pairs (hi, lo) in the `partials` buffer, and the last block
+// folds them in double-float as well, in fixed block order; only the NS + 1
+// totals handed to `finish` are FP64 (double(hi) + double(lo)).  An FP64
+// fold of ~900 blocks' partials by the last block cost ~9 us at the end of
+// the kernel.  `ticket` points to 1 + kTicketGroups zeroed counters
+// (arrive_grouped).
 template <int NS, typename Finish>
 __device__ void block_reduce_df_and_finish(const DF (&sums)[NS], float mx, double* partials,
                                            unsigned* ticket, Finish finish) {
   constexpr int NV = NS + 1;
-  // the per-warp pairs and maxima, then (last block) the fold's per-warp
-  // totals: one buffer, so the kernel's shared memory grows no more than
-  // with block_reduce_and_finish
-  constexpr int kDfBytes = 32 * NS * (int)sizeof(DF) + 32 * (int)sizeof(float);
-  constexpr int kFoldBytes = 32 * NV * (int)sizeof(double);
-  __shared__ __align__(16) unsigned char s_buf[kDfBytes > kFoldBytes ? kDfBytes : kFoldBytes];
+  __shared__ DF s_df[32][NS];
+  __shared__ float s_mx[32];
   __shared__ bool s_last;
-  DF (*s_df)[NS] = reinterpret_cast<DF (*)[NS]>(s_buf);
-  float* s_mx = reinterpret_cast<float*>(s_buf + 32 * NS * sizeof(DF));
-  double (*s_warp)[NV] = reinterpret_cast<double (*)[NV]>(s_buf);
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nthreads = blockDim.x * blockDim.y * blockDim.z;
   const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
   const int lane = tid & 31, warp = tid >> 5;
   const int nwarps = (nthreads + 31) >> 5;
+  float2* part = reinterpret_cast<float2*>(partials);
+  // this block's totals -> one partial per value
 #pragma unroll
   for (int v = 0; v < NS; ++v) {
     const DF r = warp_sum_df(sums[v]);
@@ -262,23 +284,60 @@ __device__ void block_reduce_df_and_finish(const DF (&sums)[NS], float mx, doubl
 #pragma unroll
     for (int v = 0; v < NS; ++v) {
       const DF r = warp_sum_df(lane < nwarps ? s_df[lane][v] : DF{0.f, 0.f});
-      if (lane == 0) partials[(size_t)v * nblocks + bid] = (double)r.hi + (double)r.lo;
+      if (lane == 0) part[(size_t)v * nblocks + bid] = make_float2(r.hi, r.lo);
     }
     const float mb = warp_max_f(lane < nwarps ? s_mx[lane] : -INFINITY);
     if (lane == 0) {
-      partials[(size_t)NS * nblocks + bid] = (double)mb;
-      __threadfence();
-      unsigned t = atomicAdd(ticket, 1u);
-      s_last = (t == nblocks - 1);
+      part[(size_t)NS * nblocks + bid] = make_float2(mb, 0.f);
+      s_last = arrive_grouped(ticket, bid, nblocks);
     }
   }
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  int ops[NV];
+  // last block: each thread folds its strided share b = tid, tid + nthreads,
+  // ... in that order, with the L2 loads of four shares issued before their adds
+  DF acc[NS];
+  float amx = -INFINITY;
 #pragma unroll
-  for (int v = 0; v < NV; ++v) ops[v] = v < NS ? RED_SUM : RED_MAX;
-  fold_partials_and_finish<NV>(ops, partials, ticket, nblocks, tid, nthreads, s_warp, finish);
+  for (int v = 0; v < NS; ++v) acc[v] = DF{0.f, 0.f};
+  constexpr int kFoldLoads = 4;
+  for (unsigned b0 = tid; b0 < nblocks; b0 += kFoldLoads * nthreads) {
+    float2 t[NV][kFoldLoads];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int j = 0; j < kFoldLoads; ++j) {
+        const unsigned b = b0 + j * nthreads;
+        t[v][j] = b < nblocks ? __ldcg(part + (size_t)v * nblocks + b) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+    for (int j = 0; j < kFoldLoads; ++j) {
+      if (b0 + j * nthreads >= nblocks) break;
+#pragma unroll
+      for (int v = 0; v < NS; ++v) acc[v] = df_add(acc[v], DF{t[v][j].x, t[v][j].y});
+      amx = fmaxf(amx, t[NS][j].x);
+    }
+  }
+  __syncthreads();   // s_df, s_mx of this block's own partial are read
+#pragma unroll
+  for (int v = 0; v < NS; ++v) {
+    const DF r = warp_sum_df(acc[v]);
+    if (lane == 0) s_df[warp][v] = r;
+  }
+  const float wm = warp_max_f(amx);
+  if (lane == 0) s_mx[warp] = wm;
+  __syncthreads();
+  if (warp == 0) {
+    double tot[NV];
+#pragma unroll
+    for (int v = 0; v < NS; ++v) {
+      const DF r = warp_sum_df(lane < nwarps ? s_df[lane][v] : DF{0.f, 0.f});
+      tot[v] = (double)r.hi + (double)r.lo;
+    }
+    tot[NS] = (double)warp_max_f(lane < nwarps ? s_mx[lane] : -INFINITY);
+    if (lane == 0) finish(tot);
+  }
 }
 
 }  // namespace opyx

@@ -15,7 +15,9 @@ namespace opyx {
 namespace rof {
 
 // Workspace layout (bytes): [0, 256) adaptive state, [256, 512) info record,
-// [512, 512 + kPartials) FP64 block partials, then the ticket word.
+// [512, 512 + kPartials) FP64 block partials, then 256 bytes of ticket
+// counters (one word, or 1 + kTicketGroups for the grouped arrivals of the
+// FP32 gap reductions), zeroed by opyx_rof_init.
 constexpr size_t kStateOff = 0;
 constexpr size_t kInfoOff = 256;
 constexpr int kMaxBlocks = 4096;
@@ -23,6 +25,7 @@ constexpr size_t kPartialsOff = 512;
 constexpr size_t kPartialsBytes = (size_t)kMaxBlocks * 5 * sizeof(double);
 constexpr size_t kTicketOff = kPartialsOff + kPartialsBytes;
 constexpr size_t kWsBytes = kTicketOff + 256;
+static_assert((1 + kTicketGroups) * sizeof(unsigned) <= 256, "ticket counters");
 
 static_assert(sizeof(opyx_adaptive_state) <= 256, "state record too large");
 static_assert(sizeof(opyx_rof_info) <= 256, "info record too large");
