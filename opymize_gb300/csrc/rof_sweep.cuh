@@ -530,7 +530,7 @@ OPYX_D bool sweep_rows(const Geo<float>& g, const Args<float>& a, int64_t q_beg,
 // GAP: the first sweep of a check chunk, which also computes the gap of the
 // state it reads (opyx_rof_gap_iterate) and runs the stop test on it.
 template <int C, int TW = kPipeTW, int P = kSweepP, int DP = 1, bool GAP = false>
-__global__ void __launch_bounds__(TW / P, sweep_min_blocks(TW, P))
+__global__ void __launch_bounds__(TW / P, GAP && C >= 3 ? 2 : sweep_min_blocks(TW, P))
 k_sweep(Geo<float> g, Args<float> a, int RB, double ssd_shift) {
   extern __shared__ float4 smem4[];
   __shared__ __align__(8) uint64_t mbar[kSweepMaxBars];
