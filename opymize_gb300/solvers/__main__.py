@@ -4,6 +4,11 @@ number of iterations -- a small, repeatable case for profilers:
     python -m opymize_gb300.solvers --dims 256 256 256 --iters 20
     python -m opymize_gb300.solvers --dims 2048 2048 --channels 3 --huber 0.01 --lbd 0.05
     python -m opymize_gb300.solvers --dims 512 512 --sublabel 16 --lbd 0.1 --iters 10
+    python -m opymize_gb300.solvers --dims 2048 2048 --lbd 0.1 --iters 20 --gran 10
+
+``--gran`` is the check interval (default: one check after the last
+iteration); with 2-D single sweeps each check but the last is computed by the
+first sweep of the next chunk.
 
 With ``--sublabel L`` the problem is the sublabel-lifted model of
 ``tools.lifting.sublabel_problem`` (L labels on [0, 1], 8 samples per
@@ -33,7 +38,9 @@ def main(argv=None):
     ap.add_argument("--steps", default="precond")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--sublabel", type=int, default=0)
+    ap.add_argument("--gran", type=int, default=0)
     a = ap.parse_args(argv)
+    gran = a.gran if a.gran > 0 else a.iters
     if a.sublabel:
         return sublabel(a)
     dims, C = tuple(a.dims), a.channels
@@ -42,7 +49,7 @@ def main(argv=None):
     F = HuberL1Norms(N, (C, D), a.lbd, a.huber) if a.huber > 0 else L1Norms(N, (C, D), a.lbd)
     s = PDHG(SSD(f.reshape(N, C)), F, GradientOp(dims, C, scheme="forward"))
     s.solve(steps=a.steps, precision="float", term_pd_gap=1e-300, term_maxiter=a.iters,
-            granularity=a.iters)
+            granularity=gran)
     torch().cuda.synchronize()
     print(json.dumps({"dims": list(dims), "channels": C, "path": s.path, "iters": s.info["iter"],
                       "relgap": s.info["relgap"]}))

@@ -34,6 +34,7 @@ class BatchROF(object):
 
     GRAN_RANGE = (10, 100)
     GRAN_PRIOR_ITERS = 1000   # iterations an instance is assumed to need when tuning the interval
+    PERSIST_MARGIN = 1.1      # persistent kept unless the graphs' full iteration is this much faster
 
     def __init__(self, images, lbd, huber=0.0, tol=1e-4, granularity=10, rows_per_item=None,
                  persistent=None):
@@ -241,8 +242,10 @@ class BatchROF(object):
         for one-channel batches whose mode was not fixed by `persistent`,
         also the mode: the persistent launch and the graph-captured
         per-iteration launches are both tuned and the faster iteration over
-        the whole batch is kept (the persistent launch won on a batch of 512
-        mixed sizes, the graphs on 32 equal 512^2 images)."""
+        the whole batch is kept, the persistent launch unless the graphs'
+        iteration is more than PERSIST_MARGIN times faster (the persistent
+        launch won on a batch of 512 mixed sizes, the graphs on 32 equal
+        512^2 images)."""
         if self._persistent_req is None and self.C == 1:
             self.persistent = True
             rp = self._autotune_persistent(iters)
@@ -251,7 +254,12 @@ class BatchROF(object):
             self.persistent = False
             rg = self._autotune_graphs(iters)
             tg = dict(self.tuning)
-            if tp["ms_per_iteration"] <= tg["ms_per_iteration"]:
+            # the tuning times iterations with every instance active; the
+            # persistent launch gains in the tail (no per-check host round
+            # trips or descriptor rebuilds: 512 mixed instances 3.89 s against
+            # 4.03 s with graphs at 0.756 against ~0.74 ms per full iteration),
+            # so it is kept unless the graphs are clearly faster
+            if tp["ms_per_iteration"] <= self.PERSIST_MARGIN * tg["ms_per_iteration"]:
                 self.persistent, self.rows_per_item, self.tuning, self.gran = True, rp, tp, gp
             self.tuning["mode"] = "persistent" if self.persistent else "graphs"
             self.tuning["ms_per_iteration_other_mode"] = (
