@@ -211,6 +211,29 @@ class DeviceArray(object):
         return self
 
 
+_copy_streams = []
+
+
+def get_all(arrays):
+    """Host copies of several device arrays (as DeviceArray.get), each
+    transfer on its own stream after the work queued so far, so that they
+    run on separate copy engines at once; synchronises."""
+    t = torch()
+    cur = t.cuda.current_stream()
+    while len(_copy_streams) < len(arrays):
+        _copy_streams.append(t.cuda.Stream())
+    outs = []
+    for a, st in zip(arrays, _copy_streams):
+        h = t.empty(tuple(a.t.shape), dtype=a.t.dtype, pin_memory=True)
+        st.wait_stream(cur)
+        with t.cuda.stream(st):
+            h.copy_(a.t, non_blocking=True)
+        outs.append(h)
+    for st in _copy_streams[:len(arrays)]:
+        st.synchronize()
+    return [h.numpy() for h in outs]
+
+
 def to_gpu(ary, dtype=None):
     return DeviceArray.to_gpu(ary, dtype)
 

@@ -23,7 +23,7 @@ import time
 import numpy as np
 
 from opymize_gb300 import _lib
-from opymize_gb300.gpuarray import DeviceArray, stream_ptr, torch
+from opymize_gb300.gpuarray import DeviceArray, get_all, stream_ptr, torch
 from opymize_gb300.steps import DeviceScalar, step_struct
 from opymize_gb300.linear import normest
 from opymize_gb300.linear.diff import GradientOp
@@ -254,8 +254,9 @@ class PDHG(object):
         return DeviceArray.to_gpu(i['xk'], dtype), DeviceArray.to_gpu(i['yk'], dtype)
 
     def _download(self, x, y):
-        self.itervars['xk'] = x.get().reshape(self.itervars['xk'].shape)
-        self.itervars['yk'] = y.get().reshape(self.itervars['yk'].shape)
+        xh, yh = get_all([x, y])
+        self.itervars['xk'] = xh.reshape(self.itervars['xk'].shape)
+        self.itervars['yk'] = yh.reshape(self.itervars['yk'].shape)
 
     # ------------------------------------------------------------ generic
     def _solve_generic(self, dtype, steps, term_pd_gap, term_pd_res, pd_res_mode,
@@ -473,17 +474,24 @@ class _FusedLoop(object):
     callback, a check is queued with the next chunk's iterations
     (opyx_rof_gap_iterate: the first sweep computes it from the rows it loads)
     and its record copied after that chunk; the record then arrives one chunk
-    later, so one fewer newer record is waited for.  Chunks are replayed as
-    CUDA graphs (one per kind and length).  `run` must follow opyx_rof_init,
-    which clears the check counter.
+    later, so one fewer newer record is waited for.  Chunks of a kind queued
+    more than EAGER_USES times are replayed as CUDA graphs (one per kind and
+    length).  `run` must follow opyx_rof_init, which clears the check counter.
     """
     DEPTH = 2
+    # a chunk kind is queued by direct launches this many times before it is
+    # captured: a capture costs ~0.25 ms on the host and a replay saves
+    # ~7-9 us of GPU time per 10-iteration chunk against direct (chained)
+    # launches, so short solves (the 30-iteration 2048x2048x3 headline: 7
+    # chunks) never capture and long ones do after a few chunks
+    EAGER_USES = 16
 
     def __init__(self, p, b, ws, granularity, graph=True):
         self.p, self.b, self.gran, self.use_graph = p, b, int(granularity), graph
         off = _lib.load().opyx_rof_info_offset() // 8
         self.info_dev = ws.t[off:off + len(_lib.ROF_INFO_FIELDS)]
         self.graphs = {}
+        self.uses = {}         # chunks queued per kind
         self.host = None
         self.launches = 0      # kernel launches queued so far
         self.sweeps = bool(_lib.load().opyx_rof_uses_sweep(p, b))
@@ -493,8 +501,10 @@ class _FusedLoop(object):
     def chunk(self, n, check, first=False):
         """n iterations; `check`: the gap after them; `first`: the gap of the
         state before them, fused into their first sweep (n >= 2)."""
-        if n and self.use_graph:
-            key = (n, check, first)
+        key = (n, check, first)
+        uses = self.uses.get(key, 0)
+        self.uses[key] = uses + 1
+        if n and self.use_graph and uses >= self.EAGER_USES:
             g = self.graphs.get(key)
             if g is None:
                 g = self.graphs[key] = _RofGraph(self.p, self.b, n, check, first)
