@@ -482,9 +482,11 @@ class _FusedLoop(object):
     # a chunk kind is queued by direct launches this many times before it is
     # captured: a capture costs ~0.25 ms on the host and a replay saves
     # ~7-9 us of GPU time per 10-iteration chunk against direct (chained)
-    # launches, so short solves (the 30-iteration 2048x2048x3 headline: 7
-    # chunks) never capture and long ones do after a few chunks
-    EAGER_USES = 16
+    # launches; a kind met once per solve (the first chunk) is captured from
+    # the third solve on a reused loop.  (16 direct uses measured slower on a
+    # reused loop: 2.26 against 2.18 ms for the 30-iteration 2048x2048x3 solve,
+    # whose first chunk then stayed direct and started behind the host.)
+    EAGER_USES = 2
 
     def __init__(self, p, b, ws, granularity, graph=True):
         self.p, self.b, self.gran, self.use_graph = p, b, int(granularity), graph
