@@ -211,7 +211,7 @@ class DeviceArray(object):
         return self
 
 
-_copy_streams = []
+_copy_streams = {}   # device index -> streams of get_all
 
 
 def get_all(arrays):
@@ -220,16 +220,17 @@ def get_all(arrays):
     run on separate copy engines at once; synchronises."""
     t = torch()
     cur = t.cuda.current_stream()
-    while len(_copy_streams) < len(arrays):
-        _copy_streams.append(t.cuda.Stream())
+    streams = _copy_streams.setdefault(t.cuda.current_device(), [])
+    while len(streams) < len(arrays):
+        streams.append(t.cuda.Stream())
     outs = []
-    for a, st in zip(arrays, _copy_streams):
+    for a, st in zip(arrays, streams):
         h = t.empty(tuple(a.t.shape), dtype=a.t.dtype, pin_memory=True)
         st.wait_stream(cur)
         with t.cuda.stream(st):
             h.copy_(a.t, non_blocking=True)
         outs.append(h)
-    for st in _copy_streams[:len(arrays)]:
+    for st in streams[:len(arrays)]:
         st.synchronize()
     return [h.numpy() for h in outs]
 
