@@ -254,8 +254,9 @@ OPYX_D void store_span(float* arr, const float* slot, const Geo<float>& g, int64
 // terms of row r that need only rows r - 1 and r (G(x), G*(-A^T y), |y|^2,
 // the infeasibility, the horizontal part of |A x|^2), and the vertical part of
 // row r - 1 from x_k of rows r - 1 (kept in registers) and r.  The per-pixel
-// arithmetic is that of k_gap_p; FP32 sums per thread over its run, FP64
-// across threads and CTAs (the last CTA folds them and runs the stop test).
+// arithmetic is that of k_gap_p; FP32 sums per thread over its run,
+// double-float pairs across runs, threads and CTAs (the last CTA folds them
+// and runs the stop test).
 template <int C, int P>
 struct SweepGap {
   float pG = 0.f, pF = 0.f, pGs = 0.f, pFs = 0.f, pinf = -INFINITY;   // this run
@@ -271,10 +272,10 @@ struct SweepGap {
   }
 };
 
-// Square root for the gap sums: the hardware approximation (sqrt.approx.f32,
-// relative error about 2^-23); the sums it enters carry FP32 rounding of the
-// same size, and the IEEE-rounded sqrtf doubled the instructions of the row
-// step.
+// Square root for the gap sums: the hardware approximation (sqrt.approx.f32),
+// whose error is of the order of the FP32 rounding the sums carry anyway (the
+// gap parity tests bound the effect); the IEEE-rounded sqrtf takes several
+// more instructions per call, two calls per pixel.
 OPYX_D float gap_sqrt(float v) {
   float r;
   asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
