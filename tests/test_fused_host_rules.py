@@ -191,3 +191,32 @@ def test_single_sweep_selection(lib, case):
         assert lib.opyx_rof_uses_sweep(C.byref(p), C.byref(b)) == 0
     b.y2 = (b.y2 or 0) + 4                                          # misaligned y2
     assert lib.opyx_rof_uses_sweep(C.byref(p), C.byref(b)) == 0
+
+
+@pytest.mark.parametrize("t_persist,t_graphs,want", [(0.92, 0.89, "persistent"),
+                                                      (0.756, 0.74, "persistent"),
+                                                      (1.00, 1.05, "persistent"),
+                                                      (1.20, 1.00, "graphs")])
+def test_batch_mode_choice(t_persist, t_graphs, want):
+    """BatchROF.autotune for one-channel batches without a fixed mode: both
+    modes tuned, the persistent launch kept unless the graphs' iteration with
+    every instance active is more than PERSIST_MARGIN times faster (host
+    rule; the timings are given)."""
+    from types import SimpleNamespace
+    from opymize_gb300.solvers.batch import BatchROF
+
+    def tune(ms, rows, gran):
+        def f(iters):
+            s.tuning = {"rows_per_item": rows, "ms_per_iteration": ms}
+            s.rows_per_item, s.gran = rows, gran
+            return rows
+        return f
+
+    s = SimpleNamespace(_persistent_req=None, C=1, PERSIST_MARGIN=BatchROF.PERSIST_MARGIN,
+                        tuning=None, gran=None, rows_per_item=None, persistent=None)
+    s._autotune_persistent = tune(t_persist, 32, 58)
+    s._autotune_graphs = tune(t_graphs, 8, 70)
+    rows = BatchROF.autotune(s)
+    assert s.tuning["mode"] == want and s.persistent == (want == "persistent")
+    assert (rows, s.gran) == ((32, 58) if want == "persistent" else (8, 70))
+    assert s.tuning["ms_per_iteration_other_mode"] == (t_graphs if s.persistent else t_persist)
