@@ -107,3 +107,36 @@ def test_interrupt_handler_first_sigint_recorded_second_raises():
             os.kill(os.getpid(), signal.SIGINT)
             time.sleep(0.01)
     assert signal.getsignal(signal.SIGINT) is before
+
+
+def test_split_op_parts_and_jacobian():
+    """SplitOp (opymize/operators/__init__.py:6-27): each part acts on its
+    own sub-vector (in place when y is None), and with jacobian=True the
+    result is the block-diagonal BlockOp of the parts' Jacobians."""
+    from opymize_gb300 import Variable
+    from opymize_gb300.linear import ZeroOp
+    from opymize_gb300.operators import SplitOp
+
+    class Part(object):
+        def __init__(self, n, tag):
+            self.x, self.y, self.tag, self.calls = Variable(n), Variable(n), tag, []
+            self.adjoint = self
+
+        def __call__(self, x, y=None, add=False, jacobian=False):
+            self.calls.append((x.copy(), None if y is None else y.shape, add, jacobian))
+            return self if jacobian else None
+
+    a, b = Part(3, "a"), Part(5, "b")
+    op = SplitOp([a, b])
+    assert (op.x.size, op.y.size) == (8, 8)
+    x = np.arange(8.0)
+    assert op._call_gpu(x, np.zeros(8), add=True) is None
+    np.testing.assert_array_equal(a.calls[0][0], x[:3])
+    np.testing.assert_array_equal(b.calls[0][0], x[3:])
+    assert a.calls[0][1:] == ((3,), True, False) and b.calls[0][1:] == ((5,), True, False)
+    op._call_gpu(x)                                     # in place
+    assert a.calls[1][1] is None and b.calls[1][1] is None
+    J = op._call_gpu(x, jacobian=True)
+    assert J.blocks[0][0] is a and J.blocks[1][1] is b
+    assert isinstance(J.blocks[0][1], ZeroOp) and isinstance(J.blocks[1][0], ZeroOp)
+    assert (J.blocks[0][1].y.size, J.blocks[0][1].x.size) == (3, 5)
